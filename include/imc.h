@@ -1,0 +1,255 @@
+/*
+ * imc.h -- C ABI of the GB300 Implicit Monte Carlo (IMC) particle engine.
+ *
+ * This is the drop-in boundary for the per-timestep particle path of
+ * MixedPrecisionIMC.jl.  The reference runs that path as plain Julia module
+ * functions that mutate `mesh`, `simvars` and `particles` in place:
+ *
+ *   Update.update(inputs, mesh, simvars)                 src/imc_update.jl:12
+ *   Sourcing.sourcing(mesh, simvars, particles)          src/imc_sourcing.jl:12
+ *   Transport.MC(mesh, simvars, particles)               src/imc_transport.jl:13
+ *   Transport.MC2D(mesh, simvars, particles)             src/imc_transport.jl:483
+ *   Clean.clean(particles)                               src/imc_clean.jl:6
+ *   Tally.tally(inputs, mesh, simvars, particles)        src/imc_tally.jl:11
+ *   EnergyCheck.energychecker(inputs, mesh, simvars, p)  src/imc_energycheck.jl:10
+ *   timestep(timestepping, simvars)                      src/MixedPrecisionIMC.jl:181
+ *
+ * called in that order by main(args) (src/MixedPrecisionIMC.jl:136-152, 2D
+ * :165-176).  Here each stage is one entry point acting on an opaque handle
+ * that owns all device memory (mesh state in FP64, particle state as
+ * structure-of-arrays in FP64, FP32 or FP16).  The caller keeps the input deck
+ * and the mesh geometry on the host and passes them once, as plain arrays, in
+ * an ImcDeck.
+ *
+ * Conventions
+ *   - Every function returns an int status: 0 (IMC_OK) or one of IMC_ERR_*.
+ *     Nothing throws across the ABI.  imc_last_error() gives a message.
+ *   - A handle is not thread-safe; it owns one CUDA stream and every call is
+ *     ordered on it.  Calls return once their work is complete on the GPU,
+ *     except where stated.
+ *   - 2D cell arrays are x-fastest: cell (ix, iy) is element ix + iy*nx, the
+ *     memory order of a Julia Nx-by-Ny array.  Cell indices are 0-based.
+ *   - Times, energies and all mesh quantities cross the ABI as double.
+ */
+#ifndef IMC_H_
+#define IMC_H_
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IMC_ABI_VERSION 1
+
+/* status codes */
+enum {
+    IMC_OK = 0,
+    IMC_ERR_INVALID_ARG = 1,  /* bad deck field, null pointer, size mismatch */
+    IMC_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    IMC_ERR_OOM = 3,          /* device allocation failed */
+    IMC_ERR_CAPACITY = 4,     /* particle buffer would overflow */
+    IMC_ERR_NUMERIC = 5,      /* NaN / negative tally contribution seen */
+    IMC_ERR_SEGMENT_CAP = 6,  /* a history hit the per-history segment cap */
+    IMC_ERR_NO_ENERGY = 7,    /* total source energy is zero or not finite */
+    IMC_ERR_STATE = 8,        /* call out of order (e.g. transport before sourcing) */
+    IMC_ERR_NO_DEVICE = 9,    /* no CUDA device, or not an sm_103 device */
+    IMC_ERR_TIMEOUT = 10      /* a bounded device-side wait gave up */
+};
+
+/* device error-flag bits, reported in ImcStepStats.error_flags */
+enum {
+    IMC_FLAG_NAN = 1u << 0,          /* NaN energy / distance in a history */
+    IMC_FLAG_NEG_TALLY = 1u << 1,    /* negative tally contribution dropped */
+    IMC_FLAG_SEGMENT_CAP = 1u << 2,  /* history stopped at the segment cap */
+    IMC_FLAG_CAPACITY = 1u << 3,     /* sourcing clipped at buffer capacity */
+    IMC_FLAG_NO_ENERGY = 1u << 4,    /* total energy 0 / NaN: nothing sourced */
+    IMC_FLAG_FIXPOINT_RANGE = 1u << 5,  /* tally value above the fixed-point range */
+    IMC_FLAG_SURROGATE_DOMAIN = 1u << 6 /* surrogate query outside its domain (fell back) */
+};
+
+enum { IMC_GEOM_1D = 1, IMC_GEOM_2D = 2 };
+/* particle-state precision (PRECISION deck keyword) */
+enum { IMC_FP64 = 0, IMC_FP32 = 1, IMC_FP16 = 2 };
+enum { IMC_BC_VACUUM = 0, IMC_BC_REFLECT = 1 };
+enum { IMC_TS_CONSTANT = 0, IMC_TS_RAMP = 1 };
+/* boundary slots in ImcDeck.bc: order of src/MixedPrecisionIMC.jl:121-162 */
+enum { IMC_LEFT = 0, IMC_RIGHT = 1, IMC_TOP = 2, IMC_BOTTOM = 3 };
+
+/*
+ * ImcDeck: the input deck after keyword parsing and mesh generation
+ * (src/imc_input.jl:20-129, src/constants.jl:6-15, src/imc_mesh.jl:42-259).
+ * All pointers are read during imc_create only; the caller keeps ownership.
+ */
+typedef struct ImcDeck {
+    int32_t abi_version;       /* IMC_ABI_VERSION */
+    int32_t geometry;          /* IMC_GEOM_1D / IMC_GEOM_2D (GEOMETRY) */
+    int32_t nx, ny;            /* cells; ny = 1 in 1D */
+    int32_t precision;         /* IMC_FP64 / IMC_FP32 / IMC_FP16 (PRECISION) */
+    int32_t scale_select_precision; /* precision in which the energy-scale choice of
+                                       Utilities.sorter is evaluated
+                                       (src/imc_utilities.jl:23-54); IMC_FP64 etc. */
+    const double *dx;          /* nx cell widths (DX / XMESHNODES / MESHNODES) */
+    const double *dy;          /* ny cell heights (2D only; NULL in 1D) */
+    const double *temp;        /* nx*ny initial temperature (T_INIT) */
+    const double *sigma_a_val; /* nx*ny absorption-opacity constant, already / DISTANCESCALE */
+    const double *sigma_a_pow; /* nx*ny absorption-opacity temperature power */
+    const double *sigma_s_val; /* nx*ny scattering-opacity constant, already / DISTANCESCALE */
+    const double *sigma_s_pow; /* nx*ny scattering-opacity temperature power */
+    const double *bee;         /* nx*ny heat capacity (BEE_VALS) */
+    const double *radsource;   /* nx*ny radiation source (RADSOURCE_VALS) */
+    const double *t_surface;   /* 1D: [left, right]; 2D: bottom[nx], top[nx], left[ny], right[ny] */
+    int32_t bc[4];             /* IMC_BC_* for LEFTBC, RIGHTBC, TOPBC, BOTTOMBC */
+    double phys_c, phys_a, alpha;   /* PHYS_C, PHYS_A, ALPHA */
+    int32_t n_scales;          /* number of ENERGYSCALES (1..16) */
+    const double *energyscales;/* sorted descending, as src/imc_mesh.jl:130 */
+    double distancescale;      /* DISTANCESCALE */
+    int64_t n_input, n_max;    /* NINPUT, NMAX */
+    double cellmin;            /* CELLMIN */
+    int32_t linearized;        /* LINEARIZED = TRUE */
+    int32_t marshak_opacity;   /* NAME == "MARSHAK WAVE": sigma_a = val/T^3 (src/imc_update.jl:32-34) */
+    double temp_floor;         /* opacity temperature clamp T >= temp_floor (0 = off; not in the reference) */
+    uint64_t seed;             /* SEED */
+    int32_t timestepping;      /* IMC_TS_CONSTANT / IMC_TS_RAMP (TIMESTEPPING) */
+    int32_t sort_census;       /* reorder the census by cell after each step (0 = reference order) */
+    double dt, dt0, k, dtmax, t_end;  /* DT, DT0, K, DTMAX, ENDTIME */
+    int64_t capacity;          /* particle-buffer capacity; 0 = derived from NMAX */
+    int64_t segment_cap;       /* per-history segment cap; 0 = 1e7 */
+} ImcDeck;
+
+/* One timestep's scalars, as printed by the reference each step
+ * (src/imc_energycheck.jl:31-38, src/imc_transport.jl:208). */
+typedef struct ImcStepStats {
+    double t, dt;
+    double total_energy;      /* mesh.totalenergy       (src/imc_sourcing.jl:121) */
+    double energy_dep;        /* mesh.totalenergydep    (src/imc_tally.jl:51) */
+    double rad_energy;        /* sum(radenergydens*dx)  (src/imc_energycheck.jl:26) */
+    double rad_energy_old;    /* mesh.radenergyold before this step */
+    double lost_energy;       /* mesh.lostenergy        */
+    double energy_error;      /* (E - Edep - dErad - Elost)/E (src/imc_energycheck.jl:34) */
+    int64_t n_census_in;      /* particles carried into the step */
+    int64_t n_sourced;        /* particles born this step */
+    int64_t n_census_out;     /* survivors after Clean.clean */
+    int64_t segments;         /* while-loop passes this step (src/imc_transport.jl:73) */
+    int64_t surrogate_calls;  /* thick-cell surrogate evaluations */
+    uint32_t error_flags;     /* IMC_FLAG_* bits raised during the step */
+    uint32_t step_index;      /* 0-based step counter */
+} ImcStepStats;
+
+/* Host-side particle view (structure of arrays).  1D uses t,x,mu; 2D uses
+ * t,x,y,ux,uy (direction cosines).  cell is 0-based (2D: ix + iy*nx); scale is
+ * the 0-based index into ImcDeck.energyscales.  Energies are in scaled units,
+ * as the reference stores them (src/imc_sourcing.jl:173,276). */
+typedef struct ImcParticles {
+    int64_t n;
+    double *t, *x, *y, *mu, *ux, *uy, *E, *E0;
+    int32_t *cell, *scale;
+} ImcParticles;
+
+/* cell fields for imc_get_field / imc_set_field */
+enum {
+    IMC_FIELD_TEMP = 0,        /* mesh.temp */
+    IMC_FIELD_RADENERGY = 1,   /* mesh.radenergydens */
+    IMC_FIELD_MATENERGY = 2,   /* mesh.matenergydens */
+    IMC_FIELD_FLECK = 3,       /* mesh.fleck */
+    IMC_FIELD_BETA = 4,        /* mesh.beta */
+    IMC_FIELD_SIGMA_A = 5,     /* mesh.sigma_a[:,1] */
+    IMC_FIELD_SIGMA_S = 6,     /* mesh.sigma_s[:,1] */
+    IMC_FIELD_BEE = 7,         /* mesh.bee */
+    IMC_FIELD_ENERGYDEP = 8,   /* mesh.energydep, ncells*n_scales, scale-major */
+    IMC_FIELD_EMITTED = 9,     /* mesh.emittedenergy, ncells*n_scales, scale-major */
+    IMC_FIELD_COUNT = 10
+};
+
+typedef struct ImcHandle ImcHandle;
+
+/* ---- lifetime ---------------------------------------------------------- */
+
+/* Validate the deck, allocate device state and upload the mesh.  Replaces the
+ * set-up half of main(args): src/MixedPrecisionIMC.jl:78-125 (Mesh state of
+ * src/imc_mesh.jl:10-40, SimVars of :35-51, Random.seed! of :86). */
+int imc_create(const ImcDeck *deck, ImcHandle **out);
+int imc_destroy(ImcHandle *h);
+/* Copies the last error message of h (or of the last failed imc_create when
+ * h is NULL) into buf; returns the status that produced it. */
+int imc_last_error(const ImcHandle *h, char *buf, size_t len);
+/* Returns IMC_ABI_VERSION; lets a binding check it loaded the right library. */
+int imc_abi_version(void);
+/* Device name and SM count of the current device, or IMC_ERR_NO_DEVICE. */
+int imc_device_info(char *name, size_t len, int *sm_count, int *cc_major, int *cc_minor);
+
+/* ---- per-stage entry points (one per reference function) --------------- */
+
+/* Update.update: opacities, beta, Fleck factor, FP64 (src/imc_update.jl:12-56).
+ * Uses the current dt. */
+int imc_update(ImcHandle *h);
+/* Sourcing.sourcing: emission energies, particle budget and births appended
+ * after the census (src/imc_sourcing.jl:12-370). */
+int imc_sourcing(ImcHandle *h);
+/* Transport.MC (1D, src/imc_transport.jl:13-210) or Transport.MC2D (2D,
+ * :483-732): every particle history to census, escape or cut-off; tallies
+ * energy deposition, escaped energy and census radiation energy. */
+int imc_transport(ImcHandle *h);
+/* Clean.clean: stable removal of killed particles (src/imc_clean.jl:6-19). */
+int imc_clean(ImcHandle *h);
+/* Tally.tally: material energy, temperature and radiation energy density
+ * (src/imc_tally.jl:11-149), FP64. */
+int imc_tally(ImcHandle *h);
+/* EnergyCheck.energychecker (src/imc_energycheck.jl:10-56), FP64.  Writes the
+ * relative balance error to *energy_error (may be NULL). */
+int imc_energycheck(ImcHandle *h, double *energy_error);
+/* timestep(timestepping, simvars): CONSTANT / RAMP control
+ * (src/MixedPrecisionIMC.jl:181-222).  *done = 1 once t > t_end. */
+int imc_timestep(ImcHandle *h, int *done);
+
+/* ---- whole-step / whole-run entry points -------------------------------- */
+
+/* One timestep: update -> sourcing -> transport -> clean -> tally ->
+ * energycheck -> timestep (src/MixedPrecisionIMC.jl:136-152).  stats may be
+ * NULL.  *done = 1 once t > t_end. */
+int imc_step(ImcHandle *h, ImcStepStats *stats, int *done);
+/* Run steps until t > t_end or max_steps steps ran, replaying one captured
+ * CUDA graph per step.  stats (may be NULL) receives up to max_steps entries;
+ * *n_steps the number run; *device_ms (may be NULL) the device time of the
+ * run measured with CUDA events on the handle's stream. */
+int imc_run(ImcHandle *h, int64_t max_steps, ImcStepStats *stats,
+            int64_t *n_steps, double *device_ms);
+
+/* ---- state access ------------------------------------------------------- */
+
+/* simulation clock (simvars.t, simvars.dt) and step counter */
+int imc_get_time(const ImcHandle *h, double *t, double *dt, int64_t *step_index);
+/* Overrides t and dt (the reference tests build SimVars by hand,
+ * test/runtests.jl:67). */
+int imc_set_time(ImcHandle *h, double t, double dt);
+/* number of particles in the list (census + any sourced, not yet cleaned) */
+int imc_num_particles(const ImcHandle *h, int64_t *n);
+/* copy a cell field (IMC_FIELD_*) to / from the host; count = ncells, or
+ * ncells*n_scales for ENERGYDEP / EMITTED. */
+int imc_get_field(const ImcHandle *h, int field, double *out, int64_t count);
+int imc_set_field(ImcHandle *h, int field, const double *in, int64_t count);
+/* Copy the particle list to the host; p->n on entry is the capacity of the
+ * arrays, on return the number copied (all of them, or IMC_ERR_INVALID_ARG). */
+int imc_get_particles(const ImcHandle *h, ImcParticles *p);
+/* Replace the particle list (census) with p->n host particles.  E0 < 0 marks a
+ * killed particle, as slot 8 == -1.0 does in the reference
+ * (src/imc_transport.jl:104, src/imc_clean.jl:10). */
+int imc_set_particles(ImcHandle *h, const ImcParticles *p);
+/* Most recent step's scalars. */
+int imc_get_stats(const ImcHandle *h, ImcStepStats *stats);
+/* Per-launch timing of the transport kernel.  With timing on, imc_run and
+ * imc_step bracket every transport launch with CUDA events on the handle's
+ * stream (imc_run then launches each step's kernels directly instead of
+ * replaying the captured graph). */
+int imc_set_timing(ImcHandle *h, int enable);
+/* Average device time (ms) of the transport kernel over the launches since
+ * the last call; resets the accumulator.  *launches receives the count. */
+int imc_transport_timing(ImcHandle *h, double *avg_ms, int64_t *launches);
+/* Number of kernel launches one step issues (for launch accounting). */
+int imc_kernels_per_step(const ImcHandle *h, int *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMC_H_ */

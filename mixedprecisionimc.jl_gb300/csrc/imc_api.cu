@@ -1,0 +1,945 @@
+// imc_api.cu -- the C ABI of include/imc.h: handle lifetime, one entry point
+// per reference stage, whole-step and whole-run drivers, state access.
+//
+// One handle owns one CUDA stream and all device memory of one simulation.
+// Sizes that change from step to step (census length, births) live in device
+// scalars, so the host never needs them to launch: a step is a fixed sequence
+// of launches, captured once per ping-pong parity as a CUDA graph.  The host
+// keeps an exact mirror of the simulation clock (the timestep arithmetic is
+// deterministic FP64), so it knows how many steps a run has without reading
+// the device.
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/imc.h"
+#include "imc_internal.h"
+
+using namespace imc;
+
+namespace {
+
+std::string g_create_err;
+int g_create_code = IMC_OK;
+
+struct Stage { enum { Fresh = 0, Updated, Sourced, Transported, Cleaned, Tallied, Checked }; };
+
+}  // namespace
+
+struct ImcHandle {
+    ImcDeck deck;
+    int device = 0, sm_count = 0;
+    cudaStream_t stream = nullptr;
+    int prec = 1, geometry = 1, nx = 1, ny = 1, nc = 1, K = 1, nslots = 0;
+    CellArgs ca{};
+    Scalars *d_sc = nullptr;
+    std::vector<void *> allocs;  // cell / scratch allocations
+    // particle buffers
+    PBufRaw buf[2]{};
+    std::vector<void *> pallocs;
+    int cur = 0;
+    long long capacity = 0, ntiles_cap = 0;
+    long long *tile_cnt = nullptr, *tile_off = nullptr;
+    DevStats *d_stats = nullptr;
+    long long stats_cap = 0;
+    int grid_transport = 0, block_transport = 256, grid_emit = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool timing = false;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    std::vector<cudaEvent_t> ev_pool;
+    double transport_ms = 0.0;
+    int64_t transport_launches = 0;
+    // host mirror of the clock
+    double t = 0.0, dt = 0.0;
+    int64_t step = 0;
+    bool finished = false;
+    int stage = Stage::Fresh;
+    long long n_census_host = 0;
+    ImcStepStats last{};
+    std::string err;
+    int err_code = IMC_OK;
+};
+
+namespace {
+
+int fail(ImcHandle *h, int code, const std::string &msg) {
+    if (h) { h->err = msg; h->err_code = code; }
+    else { g_create_err = msg; g_create_code = code; }
+    return code;
+}
+
+#define CK(h, call)                                                                              \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess)                                                                   \
+            return fail((h), e_ == cudaErrorMemoryAllocation ? IMC_ERR_OOM : IMC_ERR_CUDA,       \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                    \
+    } while (0)
+
+#define CKL(h)                                                                                   \
+    do {                                                                                         \
+        cudaError_t e_ = cudaGetLastError();                                                     \
+        if (e_ != cudaSuccess) return fail((h), IMC_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T> int dalloc(ImcHandle *h, T **p, size_t n, std::vector<void *> &list) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+    if (e != cudaSuccess) return fail(h, IMC_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    list.push_back(q);
+    *p = (T *)q;
+    return IMC_OK;
+}
+
+template <class T> int upload(ImcHandle *h, T **p, const T *src, size_t n) {
+    int rc = dalloc(h, p, n, h->allocs);
+    if (rc) return rc;
+    if (src && n) CK(h, cudaMemcpy(*p, src, n * sizeof(T), cudaMemcpyHostToDevice));
+    else CK(h, cudaMemset(*p, 0, std::max<size_t>(n, 1) * sizeof(T)));
+    return IMC_OK;
+}
+
+size_t state_elem(int prec) { return prec == 0 ? 8 : prec == 1 ? 4 : 2; }
+size_t e0_elem(int prec) { return prec == 0 ? 8 : 4; }
+
+int alloc_particles(ImcHandle *h, long long cap, PBufRaw out[2], std::vector<void *> &list) {
+    const size_t se = state_elem(h->prec), e0 = e0_elem(h->prec);
+    for (int b = 0; b < 2; ++b) {
+        PBufRaw &r = out[b];
+        r = PBufRaw{};
+        int rc;
+        if ((rc = dalloc(h, (char **)&r.t, se * cap, list))) return rc;
+        if ((rc = dalloc(h, (char **)&r.x, se * cap, list))) return rc;
+        if ((rc = dalloc(h, (char **)&r.ux, se * cap, list))) return rc;
+        if (h->geometry == 2) {
+            if ((rc = dalloc(h, (char **)&r.y, se * cap, list))) return rc;
+            if ((rc = dalloc(h, (char **)&r.uy, se * cap, list))) return rc;
+        }
+        if ((rc = dalloc(h, (char **)&r.E, se * cap, list))) return rc;
+        if ((rc = dalloc(h, (char **)&r.E0, e0 * cap, list))) return rc;
+        if ((rc = dalloc(h, &r.cs, cap, list))) return rc;
+        if ((rc = dalloc(h, &r.alive, cap, list))) return rc;
+    }
+    return IMC_OK;
+}
+
+void free_list(std::vector<void *> &list) {
+    for (void *p : list) cudaFree(p);
+    list.clear();
+}
+
+void drop_graphs(ImcHandle *h) {
+    for (int p = 0; p < 2; ++p)
+        if (h->graph[p]) { cudaGraphExecDestroy(h->graph[p]); h->graph[p] = nullptr; }
+}
+
+long long births_bound(const ImcHandle *h, long long n_census) {
+    const ImcDeck &d = h->deck;
+    double cm = std::max(d.cellmin, 0.0);
+    double nsrc = (double)d.n_input;
+    if (d.n_input + n_census > d.n_max) nsrc = std::max(cm, (double)(d.n_max - n_census));
+    return (long long)nsrc + (long long)h->nslots * ((long long)cm + 2) + 16;
+}
+
+int tile_alloc(ImcHandle *h) {
+    h->ntiles_cap = (h->capacity + kCompactTile - 1) / kCompactTile;
+    int rc;
+    if ((rc = dalloc(h, &h->tile_cnt, h->ntiles_cap + 1, h->pallocs))) return rc;
+    if ((rc = dalloc(h, &h->tile_off, h->ntiles_cap + 1, h->pallocs))) return rc;
+    return IMC_OK;
+}
+
+// Grow both particle buffers so that `need` particles fit; keeps the list.
+int grow(ImcHandle *h, long long need) {
+    if (need <= h->capacity) return IMC_OK;
+    long long ncap = std::max<long long>(need + need / 2, h->capacity + h->capacity / 2);
+    CK(h, cudaStreamSynchronize(h->stream));
+    Scalars sc;
+    CK(h, cudaMemcpy(&sc, h->d_sc, sizeof(Scalars), cudaMemcpyDeviceToHost));
+    const long long n = sc.n_particles;
+    PBufRaw nb[2];
+    std::vector<void *> nlist;
+    long long old_cap = h->capacity;
+    h->capacity = ncap;
+    int rc = alloc_particles(h, ncap, nb, nlist);
+    if (rc) { free_list(nlist); h->capacity = old_cap; return rc; }
+    const size_t se = state_elem(h->prec), e0 = e0_elem(h->prec);
+    const PBufRaw &o = h->buf[h->cur];
+    PBufRaw &w = nb[0];
+    if (n > 0) {
+        CK(h, cudaMemcpy(w.t, o.t, se * n, cudaMemcpyDeviceToDevice));
+        CK(h, cudaMemcpy(w.x, o.x, se * n, cudaMemcpyDeviceToDevice));
+        CK(h, cudaMemcpy(w.ux, o.ux, se * n, cudaMemcpyDeviceToDevice));
+        if (h->geometry == 2) {
+            CK(h, cudaMemcpy(w.y, o.y, se * n, cudaMemcpyDeviceToDevice));
+            CK(h, cudaMemcpy(w.uy, o.uy, se * n, cudaMemcpyDeviceToDevice));
+        }
+        CK(h, cudaMemcpy(w.E, o.E, se * n, cudaMemcpyDeviceToDevice));
+        CK(h, cudaMemcpy(w.E0, o.E0, e0 * n, cudaMemcpyDeviceToDevice));
+        CK(h, cudaMemcpy(w.cs, o.cs, 4 * n, cudaMemcpyDeviceToDevice));
+        CK(h, cudaMemcpy(w.alive, o.alive, n, cudaMemcpyDeviceToDevice));
+    }
+    free_list(h->pallocs);
+    h->pallocs = nlist;
+    h->buf[0] = nb[0];
+    h->buf[1] = nb[1];
+    h->cur = 0;
+    h->ca.capacity = ncap;
+    if ((rc = tile_alloc(h))) return rc;
+    drop_graphs(h);
+    return IMC_OK;
+}
+
+int read_scalars(ImcHandle *h, Scalars *sc) {
+    CK(h, cudaMemcpyAsync(sc, h->d_sc, sizeof(Scalars), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return IMC_OK;
+}
+
+void to_stats(const DevStats &d, ImcStepStats *s) {
+    s->t = d.t; s->dt = d.dt;
+    s->total_energy = d.total_energy;
+    s->energy_dep = d.energy_dep;
+    s->rad_energy = d.rad_energy;
+    s->rad_energy_old = d.rad_energy_old;
+    s->lost_energy = d.lost_energy;
+    s->energy_error = d.energy_error;
+    s->n_census_in = d.n_census_in;
+    s->n_sourced = d.n_sourced;
+    s->n_census_out = d.n_census_out;
+    s->segments = d.segments;
+    s->surrogate_calls = d.surrogate_calls;
+    s->error_flags = d.error_flags;
+    s->step_index = d.step_index;
+}
+
+int flags_status(ImcHandle *h, unsigned flags) {
+    if (flags & IMC_FLAG_CAPACITY) return fail(h, IMC_ERR_CAPACITY, "particle buffer capacity reached; births clipped");
+    if (flags & IMC_FLAG_SEGMENT_CAP) return fail(h, IMC_ERR_SEGMENT_CAP, "a history reached the segment cap");
+    if (flags & IMC_FLAG_NO_ENERGY) return fail(h, IMC_ERR_NO_ENERGY, "total source energy is zero or not finite");
+    if (flags & (IMC_FLAG_NAN | IMC_FLAG_FIXPOINT_RANGE))
+        return fail(h, IMC_ERR_NUMERIC, "non-finite or out-of-range tally contribution");
+    return IMC_OK;
+}
+
+// host mirror of timestep (src/MixedPrecisionIMC.jl:181-222)
+void host_timestep(const ImcDeck &d, double &t, double &dt, bool &finished) {
+    if (t == d.t_end) {
+        t = d.t_end + dt;
+    } else if (d.timestepping == IMC_TS_CONSTANT) {
+        if (t + dt > d.t_end) { dt = d.t_end - t; t = d.t_end; }
+        else t = t + dt;
+    } else {
+        if (dt < d.dtmax) {
+            dt = dt * d.k;
+            if (dt > d.dtmax) dt = d.dtmax;
+        }
+        if (t + dt > d.t_end) { dt = d.t_end - t; t = d.t_end; }
+        else t = t + dt;
+    }
+    finished = t > d.t_end;
+}
+
+// the kernel sequence of one step, asynchronous on h->stream
+int enqueue_step(ImcHandle *h, int parity, bool with_events, int ev_slot) {
+    PBufRaw src = h->buf[parity], dst = h->buf[parity ^ 1];
+    cudaStream_t st = h->stream;
+    launch_update(h->ca, h->d_sc, st);
+    launch_source(h->ca, h->d_sc, h->prec, src, h->grid_emit, st);
+    if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot], st));
+    launch_transport(h->ca, h->d_sc, h->prec, src, h->grid_transport, h->block_transport, st);
+    if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot + 1], st));
+    launch_compact(h->ca, h->d_sc, h->prec, src, dst, h->tile_cnt, h->tile_off, h->ntiles_cap, st);
+    launch_tally(h->ca, h->d_sc, st);
+    launch_energycheck(h->ca, h->d_sc, h->d_stats, h->stats_cap, st);
+    launch_timestep(h->ca, h->d_sc, st);
+    CKL(h);
+    return IMC_OK;
+}
+
+int ensure_events(ImcHandle *h, size_t pairs) {
+    while (h->ev_pool.size() < 2 * pairs) {
+        cudaEvent_t e;
+        CK(h, cudaEventCreate(&e));
+        h->ev_pool.push_back(e);
+    }
+    return IMC_OK;
+}
+
+int collect_events(ImcHandle *h, size_t pairs) {
+    for (size_t i = 0; i < pairs; ++i) {
+        float ms = 0.f;
+        CK(h, cudaEventElapsedTime(&ms, h->ev_pool[2 * i], h->ev_pool[2 * i + 1]));
+        h->transport_ms += ms;
+        h->transport_launches += 1;
+    }
+    return IMC_OK;
+}
+
+int ensure_stats(ImcHandle *h, long long n) {
+    if (h->stats_cap >= n) return IMC_OK;
+    if (h->d_stats) { cudaFree(h->d_stats); h->d_stats = nullptr; }
+    long long cap = std::max<long long>(n, 64);
+    void *p = nullptr;
+    CK(h, cudaMalloc(&p, sizeof(DevStats) * cap));
+    h->d_stats = (DevStats *)p;
+    h->stats_cap = cap;
+    drop_graphs(h);
+    return IMC_OK;
+}
+
+int capture(ImcHandle *h, int parity) {
+    if (h->graph[parity]) return IMC_OK;
+    cudaGraph_t g;
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_step(h, parity, false, 0);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(h, IMC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&h->graph[parity], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(h, IMC_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    return IMC_OK;
+}
+
+int validate(const ImcDeck *d, std::string &why) {
+    if (!d) { why = "deck is NULL"; return IMC_ERR_INVALID_ARG; }
+    if (d->abi_version != IMC_ABI_VERSION) { why = "abi_version mismatch"; return IMC_ERR_INVALID_ARG; }
+    if (d->geometry != IMC_GEOM_1D && d->geometry != IMC_GEOM_2D) { why = "geometry must be 1 or 2"; return IMC_ERR_INVALID_ARG; }
+    if (d->nx <= 0 || d->ny <= 0) { why = "nx, ny must be positive"; return IMC_ERR_INVALID_ARG; }
+    long long nc = (long long)d->nx * (d->geometry == IMC_GEOM_2D ? d->ny : 1);
+    if (nc >= (1ll << 24)) { why = "at most 2^24 - 1 cells"; return IMC_ERR_INVALID_ARG; }
+    if (d->precision < IMC_FP64 || d->precision > IMC_FP16) { why = "precision must be 0, 1 or 2"; return IMC_ERR_INVALID_ARG; }
+    if (d->scale_select_precision < IMC_FP64 || d->scale_select_precision > IMC_FP16) { why = "scale_select_precision must be 0, 1 or 2"; return IMC_ERR_INVALID_ARG; }
+    if (d->n_scales < 1 || d->n_scales > 16 || !d->energyscales) { why = "1..16 energy scales required"; return IMC_ERR_INVALID_ARG; }
+    if (!d->dx || !d->temp || !d->sigma_a_val || !d->sigma_a_pow || !d->sigma_s_val || !d->sigma_s_pow ||
+        !d->bee || !d->radsource || !d->t_surface) { why = "a mesh array is NULL"; return IMC_ERR_INVALID_ARG; }
+    if (d->geometry == IMC_GEOM_2D && !d->dy) { why = "dy is NULL in 2D"; return IMC_ERR_INVALID_ARG; }
+    for (int i = 0; i < d->nx; ++i) if (!(d->dx[i] > 0)) { why = "dx must be positive"; return IMC_ERR_INVALID_ARG; }
+    if (d->geometry == IMC_GEOM_2D)
+        for (int j = 0; j < d->ny; ++j) if (!(d->dy[j] > 0)) { why = "dy must be positive"; return IMC_ERR_INVALID_ARG; }
+    for (int k = 0; k < d->n_scales; ++k) if (!(d->energyscales[k] > 0)) { why = "energy scales must be positive"; return IMC_ERR_INVALID_ARG; }
+    if (!(d->distancescale > 0) || !(d->phys_c > 0)) { why = "PHYS_C and DISTANCESCALE must be positive"; return IMC_ERR_INVALID_ARG; }
+    if (d->timestepping == IMC_TS_CONSTANT && !(d->dt > 0)) { why = "DT must be positive"; return IMC_ERR_INVALID_ARG; }
+    if (d->timestepping == IMC_TS_RAMP && (!(d->dt0 > 0) || !(d->dtmax > 0) || !(d->k > 0))) { why = "DT0, DTMAX, K must be positive"; return IMC_ERR_INVALID_ARG; }
+    if (d->n_input < 0 || d->n_max < 0) { why = "NINPUT, NMAX must be non-negative"; return IMC_ERR_INVALID_ARG; }
+    for (int b = 0; b < (d->geometry == IMC_GEOM_2D ? 4 : 2); ++b)
+        if (d->bc[b] != IMC_BC_VACUUM && d->bc[b] != IMC_BC_REFLECT) { why = "bc must be VACUUM or REFLECT"; return IMC_ERR_INVALID_ARG; }
+    return IMC_OK;
+}
+
+int check_device(ImcHandle *h, int *dev, int *sms) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return fail(h, IMC_ERR_NO_DEVICE, "no CUDA device");
+    CK(h, cudaGetDevice(dev));
+    cudaDeviceProp p;
+    CK(h, cudaGetDeviceProperties(&p, *dev));
+    if (!(p.major == 10 && p.minor == 3))
+        return fail(h, IMC_ERR_NO_DEVICE, std::string("libimc is built for sm_103a; device is ") + p.name);
+    *sms = p.multiProcessorCount;
+    return IMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int imc_abi_version(void) { return IMC_ABI_VERSION; }
+
+int imc_device_info(char *name, size_t len, int *sm_count, int *cc_major, int *cc_minor) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return IMC_ERR_NO_DEVICE;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) return IMC_ERR_NO_DEVICE;
+    if (name && len) { std::strncpy(name, p.name, len - 1); name[len - 1] = 0; }
+    if (sm_count) *sm_count = p.multiProcessorCount;
+    if (cc_major) *cc_major = p.major;
+    if (cc_minor) *cc_minor = p.minor;
+    return IMC_OK;
+}
+
+int imc_last_error(const ImcHandle *h, char *buf, size_t len) {
+    const std::string &m = h ? h->err : g_create_err;
+    int code = h ? h->err_code : g_create_code;
+    if (buf && len) { std::strncpy(buf, m.c_str(), len - 1); buf[len - 1] = 0; }
+    return code;
+}
+
+int imc_create(const ImcDeck *d, ImcHandle **out) {
+    if (!out) return fail(nullptr, IMC_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    std::string why;
+    int rc = validate(d, why);
+    if (rc) return fail(nullptr, rc, why);
+    ImcHandle *h = new ImcHandle();
+    h->deck = *d;
+    auto bail = [&](int code) {
+        g_create_err = h->err; g_create_code = code;
+        imc_destroy(h);
+        return code;
+    };
+    if ((rc = check_device(h, &h->device, &h->sm_count))) return bail(rc);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(h, IMC_ERR_CUDA, "cudaStreamCreate failed"));
+    h->prec = d->precision;
+    h->geometry = d->geometry;
+    h->nx = d->nx;
+    h->ny = d->geometry == IMC_GEOM_2D ? d->ny : 1;
+    h->nc = h->nx * h->ny;
+    h->K = d->n_scales;
+    h->nslots = (d->geometry == IMC_GEOM_1D ? 2 : 2 * h->nx + 2 * h->ny) + 2 * h->nc;
+    const int nc = h->nc, K = h->K;
+    CellArgs &ca = h->ca;
+    ca.geometry = d->geometry; ca.nx = h->nx; ca.ny = h->ny; ca.nc = nc; ca.K = K;
+    std::vector<double> ones(std::max(nc, 1), 1.0);
+    const int nts = d->geometry == IMC_GEOM_1D ? 2 : 2 * h->nx + 2 * h->ny;
+    double *p;
+    if ((rc = upload(h, &p, d->dx, h->nx))) return bail(rc); ca.dx = p;
+    if ((rc = upload(h, &p, d->geometry == IMC_GEOM_2D ? d->dy : ones.data(), h->ny))) return bail(rc); ca.dy = p;
+    if ((rc = upload(h, &ca.temp, d->temp, nc))) return bail(rc);
+    if ((rc = upload(h, &ca.bee, d->bee, nc))) return bail(rc);
+    if ((rc = upload(h, &ca.beta, ones.data(), nc))) return bail(rc);
+    if ((rc = upload<double>(h, &ca.fleck, nullptr, nc))) return bail(rc);
+    if ((rc = upload(h, &ca.sa, d->sigma_a_val, nc))) return bail(rc);
+    if ((rc = upload(h, &ca.ss, d->sigma_s_val, nc))) return bail(rc);
+    if ((rc = upload(h, &p, d->sigma_a_val, nc))) return bail(rc); ca.sa_val = p;
+    if ((rc = upload(h, &p, d->sigma_a_pow, nc))) return bail(rc); ca.sa_pow = p;
+    if ((rc = upload(h, &p, d->sigma_s_val, nc))) return bail(rc); ca.ss_val = p;
+    if ((rc = upload(h, &p, d->sigma_s_pow, nc))) return bail(rc); ca.ss_pow = p;
+    if ((rc = upload(h, &p, d->radsource, nc))) return bail(rc); ca.radsource = p;
+    if ((rc = upload(h, &p, d->t_surface, nts))) return bail(rc); ca.tsurf = p;
+    if ((rc = upload(h, &p, d->energyscales, K))) return bail(rc); ca.scales = p;
+    if ((rc = upload<double>(h, &ca.energydep, nullptr, (size_t)K * nc))) return bail(rc);
+    if ((rc = upload<double>(h, &ca.emitted, nullptr, (size_t)K * nc))) return bail(rc);
+    if ((rc = upload<double>(h, &ca.radenergydens, nullptr, nc))) return bail(rc);
+    if ((rc = upload<double>(h, &ca.matenergydens, nullptr, nc))) return bail(rc);
+    if ((rc = upload<long long>(h, &ca.dep_acc, nullptr, 3 * (size_t)K * nc))) return bail(rc);
+    if ((rc = upload<long long>(h, &ca.rad_acc, nullptr, 3 * (size_t)K * nc))) return bail(rc);
+    if ((rc = upload<long long>(h, &ca.lost_acc, nullptr, 3 * (size_t)K))) return bail(rc);
+    ca.nslots = h->nslots;
+    if ((rc = upload<double>(h, &ca.slot_e, nullptr, h->nslots))) return bail(rc);
+    if ((rc = upload<double>(h, &ca.slot_s, nullptr, h->nslots))) return bail(rc);
+    if ((rc = upload<double>(h, &ca.slot_nrg, nullptr, h->nslots))) return bail(rc);
+    if ((rc = upload<int>(h, &ca.slot_j, nullptr, h->nslots))) return bail(rc);
+    if ((rc = upload<long long>(h, &ca.slot_n, nullptr, h->nslots))) return bail(rc);
+    if ((rc = upload<long long>(h, &ca.slot_off, nullptr, h->nslots))) return bail(rc);
+    for (int b = 0; b < 4; ++b) ca.bc[b] = d->bc[b];
+    ca.c = d->phys_c; ca.a = d->phys_a; ca.alpha = d->alpha; ca.ds = d->distancescale;
+    ca.temp_floor = d->temp_floor; ca.cellmin = d->cellmin;
+    ca.linearized = d->linearized ? 1 : 0; ca.marshak = d->marshak_opacity ? 1 : 0;
+    ca.sel_prec = d->scale_select_precision;
+    ca.timestepping = d->timestepping;
+    ca.n_input = d->n_input; ca.n_max = d->n_max;
+    ca.seg_cap = d->segment_cap > 0 ? d->segment_cap : 10000000;
+    ca.seed = d->seed;
+    double dxmin = *std::min_element(d->dx, d->dx + h->nx);
+    double dymin = d->geometry == IMC_GEOM_2D ? *std::min_element(d->dy, d->dy + h->ny) : 1.0;
+    ca.vol_min = dxmin * dymin;
+    ca.scale_min = *std::min_element(d->energyscales, d->energyscales + K);
+    ca.t_end = d->t_end; ca.dtmax = d->dtmax; ca.kfac = d->k;
+    // particle buffers
+    long long cap = d->capacity > 0 ? d->capacity : (d->n_max + 2 * births_bound(h, 0));
+    if (cap < 1024) cap = 1024;
+    h->capacity = cap;
+    ca.capacity = cap;
+    if ((rc = alloc_particles(h, cap, h->buf, h->pallocs))) return bail(rc);
+    if ((rc = tile_alloc(h))) return bail(rc);
+    // scalars
+    Scalars sc{};
+    h->t = 0.0;
+    h->dt = d->timestepping == IMC_TS_RAMP ? d->dt0 : d->dt;
+    sc.t = h->t; sc.dt = h->dt;
+    void *q = nullptr;
+    if (cudaMalloc(&q, sizeof(Scalars)) != cudaSuccess) return bail(fail(h, IMC_ERR_OOM, "cudaMalloc scalars"));
+    h->allocs.push_back(q);
+    h->d_sc = (Scalars *)q;
+    if (cudaMemcpy(h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(fail(h, IMC_ERR_CUDA, "upload scalars"));
+    if ((rc = ensure_stats(h, 64))) return bail(rc);
+    // launch shapes: persistent grids sized by occupancy on this GPU
+    int smem = transport_smem_bytes(ca, h->prec);
+    const void *kp = transport_kernel_ptr(ca, h->prec);
+    if (smem > 227 * 1024) return bail(fail(h, IMC_ERR_INVALID_ARG, "mesh too large for the shared-memory transport table"));
+    if (smem > 48 * 1024)
+        if (cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+            return bail(fail(h, IMC_ERR_CUDA, "cudaFuncSetAttribute(smem)"));
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp, h->block_transport, smem) != cudaSuccess || per_sm < 1)
+        return bail(fail(h, IMC_ERR_CUDA, "transport kernel cannot be resident"));
+    h->grid_transport = h->sm_count * per_sm;
+    h->grid_emit = h->sm_count * 4;
+    if (cudaEventCreate(&h->ev[0]) != cudaSuccess || cudaEventCreate(&h->ev[1]) != cudaSuccess)
+        return bail(fail(h, IMC_ERR_CUDA, "cudaEventCreate"));
+    *out = h;
+    return IMC_OK;
+}
+
+int imc_destroy(ImcHandle *h) {
+    if (!h) return IMC_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    drop_graphs(h);
+    for (auto e : h->ev_pool) cudaEventDestroy(e);
+    for (int i = 0; i < 2; ++i) if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+    if (h->d_stats) cudaFree(h->d_stats);
+    free_list(h->pallocs);
+    free_list(h->allocs);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return IMC_OK;
+}
+
+int imc_update(ImcHandle *h) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    launch_update(h->ca, h->d_sc, h->stream);
+    CKL(h);
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->stage = Stage::Updated;
+    return IMC_OK;
+}
+
+int imc_sourcing(ImcHandle *h) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    Scalars sc;
+    int rc = read_scalars(h, &sc);
+    if (rc) return rc;
+    if ((rc = grow(h, sc.n_particles + births_bound(h, sc.n_particles)))) return rc;
+    launch_source(h->ca, h->d_sc, h->prec, h->buf[h->cur], h->grid_emit, h->stream);
+    CKL(h);
+    if ((rc = read_scalars(h, &sc))) return rc;
+    h->stage = Stage::Sourced;
+    if (sc.flags & (IMC_FLAG_CAPACITY | IMC_FLAG_NO_ENERGY)) return flags_status(h, sc.flags);
+    return IMC_OK;
+}
+
+int imc_transport(ImcHandle *h) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    if (h->stage != Stage::Sourced) launch_prepare_transport(h->ca, h->d_sc, h->stream);
+    if (h->timing) CK(h, cudaEventRecord(h->ev[0], h->stream));
+    launch_transport(h->ca, h->d_sc, h->prec, h->buf[h->cur], h->grid_transport, h->block_transport, h->stream);
+    CKL(h);
+    if (h->timing) {
+        CK(h, cudaEventRecord(h->ev[1], h->stream));
+        CK(h, cudaEventSynchronize(h->ev[1]));
+        float ms = 0;
+        CK(h, cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
+        h->transport_ms += ms;
+        h->transport_launches += 1;
+    }
+    Scalars sc;
+    int rc = read_scalars(h, &sc);
+    if (rc) return rc;
+    h->stage = Stage::Transported;
+    return flags_status(h, sc.flags & (IMC_FLAG_SEGMENT_CAP | IMC_FLAG_NAN | IMC_FLAG_FIXPOINT_RANGE));
+}
+
+int imc_clean(ImcHandle *h) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    launch_compact(h->ca, h->d_sc, h->prec, h->buf[h->cur], h->buf[h->cur ^ 1], h->tile_cnt, h->tile_off,
+                   h->ntiles_cap, h->stream);
+    CKL(h);
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->cur ^= 1;
+    h->stage = Stage::Cleaned;
+    return IMC_OK;
+}
+
+int imc_tally(ImcHandle *h) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    launch_tally(h->ca, h->d_sc, h->stream);
+    CKL(h);
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->stage = Stage::Tallied;
+    return IMC_OK;
+}
+
+int imc_energycheck(ImcHandle *h, double *energy_error) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    launch_energycheck(h->ca, h->d_sc, h->d_stats, h->stats_cap, h->stream);
+    CKL(h);
+    Scalars sc;
+    int rc = read_scalars(h, &sc);
+    if (rc) return rc;
+    DevStats ds;
+    CK(h, cudaMemcpy(&ds, h->d_stats + (sc.step % (unsigned long long)h->stats_cap), sizeof(DevStats),
+                     cudaMemcpyDeviceToHost));
+    to_stats(ds, &h->last);
+    if (energy_error) *energy_error = sc.energy_err;
+    h->stage = Stage::Checked;
+    return IMC_OK;
+}
+
+int imc_timestep(ImcHandle *h, int *done) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    launch_timestep(h->ca, h->d_sc, h->stream);
+    CKL(h);
+    CK(h, cudaStreamSynchronize(h->stream));
+    bool fin;
+    host_timestep(h->deck, h->t, h->dt, fin);
+    h->finished = fin;
+    h->step += 1;
+    h->stage = Stage::Fresh;
+    if (done) *done = fin ? 1 : 0;
+    return IMC_OK;
+}
+
+int imc_step(ImcHandle *h, ImcStepStats *stats, int *done) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    if (h->finished) { if (done) *done = 1; return IMC_OK; }
+    Scalars sc;
+    int rc = read_scalars(h, &sc);
+    if (rc) return rc;
+    if ((rc = grow(h, sc.n_particles + births_bound(h, sc.n_particles)))) return rc;
+    if (h->timing) {
+        if ((rc = ensure_events(h, 1))) return rc;
+        if ((rc = enqueue_step(h, h->cur, true, 0))) return rc;
+    } else {
+        if ((rc = capture(h, h->cur))) return rc;
+        CK(h, cudaGraphLaunch(h->graph[h->cur], h->stream));
+    }
+    if ((rc = read_scalars(h, &sc))) return rc;
+    if (h->timing && (rc = collect_events(h, 1))) return rc;
+    h->cur ^= 1;
+    DevStats ds;
+    CK(h, cudaMemcpy(&ds, h->d_stats + ((sc.step - 1u) % (unsigned long long)h->stats_cap), sizeof(DevStats),
+                     cudaMemcpyDeviceToHost));
+    to_stats(ds, &h->last);
+    if (stats) *stats = h->last;
+    bool fin;
+    host_timestep(h->deck, h->t, h->dt, fin);
+    h->finished = fin;
+    h->step += 1;
+    h->stage = Stage::Fresh;
+    if (done) *done = fin ? 1 : 0;
+    return flags_status(h, ds.error_flags);
+}
+
+int imc_run(ImcHandle *h, int64_t max_steps, ImcStepStats *stats, int64_t *n_steps, double *device_ms) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    if (n_steps) *n_steps = 0;
+    if (device_ms) *device_ms = 0.0;
+    // steps this run will take, from the host clock mirror
+    std::vector<std::pair<double, double>> sched;
+    {
+        double t = h->t, dt = h->dt;
+        bool fin = h->finished;
+        while (!fin && (int64_t)sched.size() < max_steps) {
+            sched.emplace_back(t, dt);
+            host_timestep(h->deck, t, dt, fin);
+        }
+    }
+    const int64_t N = (int64_t)sched.size();
+    if (N == 0) return IMC_OK;
+    int rc;
+    if ((rc = ensure_stats(h, N))) return rc;
+    Scalars sc;
+    if ((rc = read_scalars(h, &sc))) return rc;
+    // first stats slot of this run
+    const unsigned long long slot0 = sc.step;
+    CK(h, cudaEventRecord(h->ev[0], h->stream));
+    int64_t done_steps = 0;
+    long long n_census = sc.n_particles;
+    while (done_steps < N) {
+        // largest chunk whose worst-case births fit the buffers
+        int64_t m = 0;
+        long long bound = n_census;
+        while (m < 64 && done_steps + m < N) {
+            long long nb = bound + births_bound(h, bound);
+            if (nb > h->capacity) break;
+            bound = nb;
+            ++m;
+        }
+        if (m == 0) {
+            CK(h, cudaEventRecord(h->ev[1], h->stream));
+            if ((rc = grow(h, n_census + 4 * births_bound(h, n_census)))) return rc;
+            continue;
+        }
+        if (h->timing) {
+            if ((rc = ensure_events(h, (size_t)m))) return rc;
+            for (int64_t s = 0; s < m; ++s) {
+                if ((rc = enqueue_step(h, h->cur, true, (int)s))) return rc;
+                h->cur ^= 1;
+            }
+        } else {
+            for (int64_t s = 0; s < m; ++s) {
+                if ((rc = capture(h, h->cur))) return rc;
+                CK(h, cudaGraphLaunch(h->graph[h->cur], h->stream));
+                h->cur ^= 1;
+            }
+        }
+        done_steps += m;
+        if ((rc = read_scalars(h, &sc))) return rc;
+        if (h->timing && (rc = collect_events(h, (size_t)m))) return rc;
+        n_census = sc.n_particles;
+        if (sc.flags & (IMC_FLAG_CAPACITY | IMC_FLAG_SEGMENT_CAP | IMC_FLAG_NAN | IMC_FLAG_FIXPOINT_RANGE | IMC_FLAG_NO_ENERGY))
+            break;
+    }
+    CK(h, cudaEventRecord(h->ev[1], h->stream));
+    CK(h, cudaEventSynchronize(h->ev[1]));
+    float ms = 0.f;
+    CK(h, cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
+    if (device_ms) *device_ms = ms;
+    // host clock mirror and statistics
+    std::vector<DevStats> ds((size_t)done_steps);
+    for (int64_t s = 0; s < done_steps; ++s) {
+        unsigned long long slot = (slot0 + (unsigned long long)s) % (unsigned long long)h->stats_cap;
+        CK(h, cudaMemcpy(&ds[s], h->d_stats + slot, sizeof(DevStats), cudaMemcpyDeviceToHost));
+    }
+    unsigned allflags = 0;
+    for (int64_t s = 0; s < done_steps; ++s) {
+        if (stats) to_stats(ds[s], &stats[s]);
+        allflags |= ds[s].error_flags;
+        bool fin;
+        host_timestep(h->deck, h->t, h->dt, fin);
+        h->finished = fin;
+        h->step += 1;
+    }
+    if (done_steps > 0) to_stats(ds[done_steps - 1], &h->last);
+    h->stage = Stage::Fresh;
+    if (n_steps) *n_steps = done_steps;
+    return flags_status(h, allflags);
+}
+
+int imc_get_time(const ImcHandle *h, double *t, double *dt, int64_t *step_index) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    if (t) *t = h->t;
+    if (dt) *dt = h->dt;
+    if (step_index) *step_index = h->step;
+    return IMC_OK;
+}
+
+int imc_set_time(ImcHandle *h, double t, double dt) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    Scalars sc;
+    int rc = read_scalars(h, &sc);
+    if (rc) return rc;
+    sc.t = t; sc.dt = dt;
+    sc.finished = t > h->deck.t_end ? 1 : 0;
+    CK(h, cudaMemcpy(h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice));
+    h->t = t; h->dt = dt; h->finished = t > h->deck.t_end;
+    return IMC_OK;
+}
+
+int imc_num_particles(const ImcHandle *h, int64_t *n) {
+    if (!h || !n) return IMC_ERR_INVALID_ARG;
+    Scalars sc;
+    int rc = read_scalars(const_cast<ImcHandle *>(h), &sc);
+    if (rc) return rc;
+    *n = sc.n_particles;
+    return IMC_OK;
+}
+
+static double *field_ptr(const ImcHandle *h, int field, int64_t *count) {
+    const CellArgs &ca = h->ca;
+    *count = h->nc;
+    switch (field) {
+        case IMC_FIELD_TEMP: return ca.temp;
+        case IMC_FIELD_RADENERGY: return ca.radenergydens;
+        case IMC_FIELD_MATENERGY: return ca.matenergydens;
+        case IMC_FIELD_FLECK: return ca.fleck;
+        case IMC_FIELD_BETA: return ca.beta;
+        case IMC_FIELD_SIGMA_A: return ca.sa;
+        case IMC_FIELD_SIGMA_S: return ca.ss;
+        case IMC_FIELD_BEE: return ca.bee;
+        case IMC_FIELD_ENERGYDEP: *count = (int64_t)h->nc * h->K; return ca.energydep;
+        case IMC_FIELD_EMITTED: *count = (int64_t)h->nc * h->K; return ca.emitted;
+        default: return nullptr;
+    }
+}
+
+int imc_get_field(const ImcHandle *h, int field, double *out, int64_t count) {
+    if (!h || !out) return IMC_ERR_INVALID_ARG;
+    ImcHandle *hh = const_cast<ImcHandle *>(h);
+    int64_t n;
+    double *p = field_ptr(h, field, &n);
+    if (!p) return fail(hh, IMC_ERR_INVALID_ARG, "unknown field");
+    if (n != count) return fail(hh, IMC_ERR_INVALID_ARG, "field size mismatch");
+    CK(hh, cudaStreamSynchronize(h->stream));
+    CK(hh, cudaMemcpy(out, p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    return IMC_OK;
+}
+
+int imc_set_field(ImcHandle *h, int field, const double *in, int64_t count) {
+    if (!h || !in) return IMC_ERR_INVALID_ARG;
+    int64_t n;
+    double *p = field_ptr(h, field, &n);
+    if (!p) return fail(h, IMC_ERR_INVALID_ARG, "unknown field");
+    if (n != count) return fail(h, IMC_ERR_INVALID_ARG, "field size mismatch");
+    CK(h, cudaStreamSynchronize(h->stream));
+    CK(h, cudaMemcpy(p, in, sizeof(double) * n, cudaMemcpyHostToDevice));
+    return IMC_OK;
+}
+
+int imc_get_particles(const ImcHandle *hc, ImcParticles *p) {
+    ImcHandle *h = const_cast<ImcHandle *>(hc);
+    if (!h || !p) return IMC_ERR_INVALID_ARG;
+    Scalars sc;
+    int rc = read_scalars(h, &sc);
+    if (rc) return rc;
+    const long long n = sc.n_particles;
+    if (n > p->n) return fail(h, IMC_ERR_INVALID_ARG, "particle arrays too small");
+    const PBufRaw &b = h->buf[h->cur];
+    const size_t se = state_elem(h->prec), e0 = e0_elem(h->prec);
+    std::vector<unsigned char> t(se * n), x(se * n), y(se * n), ux(se * n), uy(se * n), E(se * n), E0(e0 * n);
+    std::vector<int32_t> cs(n);
+    std::vector<uint8_t> alive(n);
+    if (n > 0) {
+        CK(h, cudaMemcpy(t.data(), b.t, se * n, cudaMemcpyDeviceToHost));
+        CK(h, cudaMemcpy(x.data(), b.x, se * n, cudaMemcpyDeviceToHost));
+        CK(h, cudaMemcpy(ux.data(), b.ux, se * n, cudaMemcpyDeviceToHost));
+        if (h->geometry == 2) {
+            CK(h, cudaMemcpy(y.data(), b.y, se * n, cudaMemcpyDeviceToHost));
+            CK(h, cudaMemcpy(uy.data(), b.uy, se * n, cudaMemcpyDeviceToHost));
+        }
+        CK(h, cudaMemcpy(E.data(), b.E, se * n, cudaMemcpyDeviceToHost));
+        CK(h, cudaMemcpy(E0.data(), b.E0, e0 * n, cudaMemcpyDeviceToHost));
+        CK(h, cudaMemcpy(cs.data(), b.cs, 4 * n, cudaMemcpyDeviceToHost));
+        CK(h, cudaMemcpy(alive.data(), b.alive, n, cudaMemcpyDeviceToHost));
+    }
+    auto rd = [&](const std::vector<unsigned char> &v, long long i) -> double {
+        if (h->prec == 0) return ((const double *)v.data())[i];
+        if (h->prec == 1) return (double)((const float *)v.data())[i];
+        return (double)__half2float(((const __half *)v.data())[i]);
+    };
+    auto rd0 = [&](long long i) -> double {
+        if (h->prec == 0) return ((const double *)E0.data())[i];
+        return (double)((const float *)E0.data())[i];
+    };
+    for (long long i = 0; i < n; ++i) {
+        const int cell = cs[i] & 0xFFFFFF, k = cs[i] >> 24;
+        const int ix = h->geometry == 1 ? cell : cell % h->nx;
+        const int iy = h->geometry == 1 ? 0 : cell / h->nx;
+        double vt = rd(t, i), vx = rd(x, i), vy = h->geometry == 2 ? rd(y, i) : 0.0;
+        double vE = rd(E, i), vE0 = rd0(i);
+        if (h->prec == 2) {
+            float dxs = (float)h->deck.dx[ix] * (float)h->deck.distancescale;
+            vx = (double)((float)vx * dxs);
+            if (h->geometry == 2) vy = (double)((float)vy * ((float)h->deck.dy[iy] * (float)h->deck.distancescale));
+            vt = (double)((float)vt * (float)h->dt);
+            vE = (double)((float)vE * (float)vE0);
+        }
+        if (p->t) p->t[i] = vt;
+        if (p->x) p->x[i] = vx;
+        if (p->y) p->y[i] = vy;
+        if (h->geometry == 1) { if (p->mu) p->mu[i] = rd(ux, i); }
+        else { if (p->ux) p->ux[i] = rd(ux, i); if (p->uy) p->uy[i] = rd(uy, i); }
+        if (p->E) p->E[i] = vE;
+        if (p->E0) p->E0[i] = alive[i] ? vE0 : -1.0;
+        if (p->cell) p->cell[i] = cell;
+        if (p->scale) p->scale[i] = k;
+    }
+    p->n = n;
+    return IMC_OK;
+}
+
+int imc_set_particles(ImcHandle *h, const ImcParticles *p) {
+    if (!h || !p || p->n < 0 || !p->E || !p->E0 || !p->cell) return IMC_ERR_INVALID_ARG;
+    const long long n = p->n;
+    int rc;
+    if ((rc = grow(h, n + births_bound(h, n)))) return rc;
+    CK(h, cudaStreamSynchronize(h->stream));
+    const int prec = h->prec;
+    const size_t se = state_elem(prec), e0s = e0_elem(prec);
+    std::vector<unsigned char> t(se * n), x(se * n), y(se * n), ux(se * n), uy(se * n), E(se * n), E0(e0s * n);
+    std::vector<int32_t> cs(n);
+    std::vector<uint8_t> alive(n);
+    double emax = 0.0;
+    auto wr = [&](std::vector<unsigned char> &v, long long i, double val) {
+        if (prec == 0) ((double *)v.data())[i] = val;
+        else if (prec == 1) ((float *)v.data())[i] = (float)val;
+        else ((__half *)v.data())[i] = __float2half_rn((float)val);
+    };
+    for (long long i = 0; i < n; ++i) {
+        const int cell = p->cell[i];
+        if (cell < 0 || cell >= h->nc) return fail(h, IMC_ERR_INVALID_ARG, "particle cell out of range");
+        const int k = p->scale ? p->scale[i] : 0;
+        if (k < 0 || k >= h->K) return fail(h, IMC_ERR_INVALID_ARG, "particle scale index out of range");
+        const int ix = h->geometry == 1 ? cell : cell % h->nx;
+        const int iy = h->geometry == 1 ? 0 : cell / h->nx;
+        const double vt = p->t ? p->t[i] : 0.0, vx = p->x ? p->x[i] : 0.0, vy = p->y ? p->y[i] : 0.0;
+        const double vE = p->E[i], vE0 = p->E0[i];
+        double dirx = h->geometry == 1 ? (p->mu ? p->mu[i] : 0.0) : (p->ux ? p->ux[i] : 0.0);
+        double diry = h->geometry == 2 && p->uy ? p->uy[i] : 0.0;
+        alive[i] = vE0 >= 0.0 ? 1 : 0;
+        cs[i] = cell | (k << 24);
+        if (prec == 2) {
+            float dxs = (float)h->deck.dx[ix] * (float)h->deck.distancescale;
+            wr(x, i, (double)((float)vx / dxs));
+            if (h->geometry == 2) wr(y, i, (double)((float)vy / ((float)h->deck.dy[iy] * (float)h->deck.distancescale)));
+            wr(t, i, (double)((float)vt / (float)h->dt));
+            ((float *)E0.data())[i] = (float)vE0;
+            float ef = (float)vE / (float)vE0;
+            wr(E, i, (double)ef);
+            if (alive[i]) emax = std::max(emax, (double)(__half2float(__float2half_rn(ef)) * (float)vE0));
+        } else {
+            wr(t, i, vt); wr(x, i, vx); wr(y, i, vy); wr(E, i, vE);
+            if (prec == 0) ((double *)E0.data())[i] = vE0;
+            else ((float *)E0.data())[i] = (float)vE0;
+            if (alive[i]) emax = std::max(emax, prec == 0 ? vE : (double)(float)vE);
+        }
+        wr(ux, i, dirx);
+        wr(uy, i, diry);
+    }
+    const PBufRaw &b = h->buf[h->cur];
+    if (n > 0) {
+        CK(h, cudaMemcpy(b.t, t.data(), se * n, cudaMemcpyHostToDevice));
+        CK(h, cudaMemcpy(b.x, x.data(), se * n, cudaMemcpyHostToDevice));
+        CK(h, cudaMemcpy(b.ux, ux.data(), se * n, cudaMemcpyHostToDevice));
+        if (h->geometry == 2) {
+            CK(h, cudaMemcpy(b.y, y.data(), se * n, cudaMemcpyHostToDevice));
+            CK(h, cudaMemcpy(b.uy, uy.data(), se * n, cudaMemcpyHostToDevice));
+        }
+        CK(h, cudaMemcpy(b.E, E.data(), se * n, cudaMemcpyHostToDevice));
+        CK(h, cudaMemcpy(b.E0, E0.data(), e0s * n, cudaMemcpyHostToDevice));
+        CK(h, cudaMemcpy(b.cs, cs.data(), 4 * n, cudaMemcpyHostToDevice));
+        CK(h, cudaMemcpy(b.alive, alive.data(), n, cudaMemcpyHostToDevice));
+    }
+    Scalars sc;
+    if ((rc = read_scalars(h, &sc))) return rc;
+    sc.n_census = n;
+    sc.n_particles = n;
+    union { double d; unsigned long long u; } cv;
+    cv.d = emax;
+    sc.emax_census_bits = cv.u;
+    CK(h, cudaMemcpy(h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice));
+    h->stage = Stage::Fresh;
+    return IMC_OK;
+}
+
+int imc_get_stats(const ImcHandle *h, ImcStepStats *stats) {
+    if (!h || !stats) return IMC_ERR_INVALID_ARG;
+    *stats = h->last;
+    return IMC_OK;
+}
+
+int imc_set_timing(ImcHandle *h, int enable) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    h->timing = enable != 0;
+    return IMC_OK;
+}
+
+int imc_transport_timing(ImcHandle *h, double *avg_ms, int64_t *launches) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    if (avg_ms) *avg_ms = h->transport_launches ? h->transport_ms / (double)h->transport_launches : 0.0;
+    if (launches) *launches = h->transport_launches;
+    h->transport_ms = 0.0;
+    h->transport_launches = 0;
+    return IMC_OK;
+}
+
+int imc_kernels_per_step(const ImcHandle *h, int *count) {
+    if (!h || !count) return IMC_ERR_INVALID_ARG;
+    // update, source x3, transport, compact x4, tally, energycheck, timestep
+    *count = 12;
+    return IMC_OK;
+}
+
+}  // extern "C"

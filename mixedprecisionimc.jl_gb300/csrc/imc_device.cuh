@@ -1,0 +1,304 @@
+// imc_device.cuh -- device-side building blocks of the IMC engine (sm_103a).
+//
+//  * Philox-4x32-10 (Salmon et al., SC'11) keyed (SEED, step, particle index,
+//    stage): every history draws its own reproducible stream, independent of
+//    which thread runs it.
+//  * Julia-semantics helpers used by the restated reference arithmetic
+//    (NaN-propagating min, isless ordering for the sorter).
+//  * Utilities.sorter (src/imc_utilities.jl:23-54) as a device function.
+//  * Exact fixed-point tally accumulation: a non-negative double v is scaled by
+//    2^-b (b fixed per step and tally) and rounded to a 96-bit integer split in
+//    three 32-bit limbs, each added to its own 64-bit accumulator.  Integer
+//    addition is associative, so the tally does not depend on the order in
+//    which histories finish: GPU runs are bit-reproducible run to run.
+#pragma once
+#include <cstdint>
+#include <cstring>
+#include <cuda_fp16.h>
+
+#ifndef IMC_HD
+#define IMC_HD __host__ __device__ __forceinline__
+#endif
+
+namespace imc {
+
+// ------------------------------------------------------------------ Philox
+constexpr uint32_t kPhiloxM0 = 0xD2511F53u;
+constexpr uint32_t kPhiloxM1 = 0xCD9E8D57u;
+constexpr uint32_t kPhiloxW0 = 0x9E3779B9u;
+constexpr uint32_t kPhiloxW1 = 0xBB67AE85u;
+
+enum : uint32_t { kStageTransport = 0, kStageSource = 1 };
+
+IMC_HD void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+                           uint32_t out[4]) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+#ifdef __CUDA_ARCH__
+        uint32_t lo0 = kPhiloxM0 * c0, hi0 = __umulhi(kPhiloxM0, c0);
+        uint32_t lo1 = kPhiloxM1 * c2, hi1 = __umulhi(kPhiloxM1, c2);
+#else
+        uint64_t p0 = (uint64_t)kPhiloxM0 * c0, p1 = (uint64_t)kPhiloxM1 * c2;
+        uint32_t lo0 = (uint32_t)p0, hi0 = (uint32_t)(p0 >> 32);
+        uint32_t lo1 = (uint32_t)p1, hi1 = (uint32_t)(p1 >> 32);
+#endif
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += kPhiloxW0; k1 += kPhiloxW1;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// One history's stream: counter {block, step, pid, stage}, key = SEED.
+struct Stream {
+    uint32_t k0, k1, step, pid, stage, block;
+    uint32_t buf[4];
+    int idx;
+    IMC_HD void init(uint64_t seed, uint32_t step_, uint32_t pid_, uint32_t stage_) {
+        k0 = (uint32_t)seed; k1 = (uint32_t)(seed >> 32);
+        step = step_; pid = pid_; stage = stage_; block = 0; idx = 4;
+    }
+    IMC_HD uint32_t next() {
+        if (idx == 4) {
+            philox4x32_10(block, step, pid, stage, k0, k1, buf);
+            block += 1u;
+            idx = 0;
+        }
+        // buf is indexed dynamically; keep it in registers via a select chain
+        uint32_t v = idx == 0 ? buf[0] : idx == 1 ? buf[1] : idx == 2 ? buf[2] : buf[3];
+        ++idx;
+        return v;
+    }
+};
+
+// uniform [0,1) and exponential variates, per arithmetic type
+template <class T> struct Rand;
+template <> struct Rand<float> {
+    static IMC_HD float u(Stream &s) { return (float)(s.next() >> 8) * 0x1p-24f; }
+    static IMC_HD float exp1(Stream &s) {
+        float v = (float)((s.next() >> 8) + 1u) * 0x1p-24f;
+        return -logf(v);
+    }
+};
+template <> struct Rand<double> {
+    static IMC_HD double u(Stream &s) {
+        uint64_t hi = s.next(), lo = s.next();
+        return (double)(((hi << 32) | lo) >> 11) * 0x1p-53;
+    }
+    static IMC_HD double exp1(Stream &s) {
+        uint64_t hi = s.next(), lo = s.next();
+        double v = (double)((((hi << 32) | lo) >> 11) + 1u) * 0x1p-53;
+        return -log(v);
+    }
+};
+
+// ------------------------------------------------------- Julia semantics
+template <class T> IMC_HD T jmin(T a, T b) {
+    if (a != a) return a;
+    if (b != b) return b;
+    return b < a ? b : a;
+}
+IMC_HD bool jisless(double a, double b) {
+    bool an = a != a, bn = b != b;
+    if (an || bn) return !an && bn;
+    if (a < b) return true;
+    if (a == b) return signbit(a) && !signbit(b);
+    return false;
+}
+
+// precision tags for the sorter's scale choice
+template <int P> struct SelType;
+template <> struct SelType<0> { typedef double T; };
+template <> struct SelType<1> { typedef float T; };
+
+IMC_HD bool sel_finite_half(float v) {
+    // binary16 overflow threshold: 65520 rounds to +inf
+    return v == v && fabsf(v) < 65520.0f;
+}
+
+// Utilities.sorter (src/imc_utilities.jl:23-54): append scale j, sort
+// ascending, multiply smallest by largest pairwise; the first scale whose
+// product is finite in the selection precision wins.  Returns the FP64
+// product; *jout = -1 if no scale works.  n <= 15.
+template <int SEL>
+IMC_HD double sorter(const double *vals, int n, const double *scales, int nsc, int *jout) {
+    double arr[16];
+    for (int j = 0; j < nsc; ++j) {
+        int m = n + 1;
+        for (int i = 0; i < n; ++i) arr[i] = vals[i];
+        arr[n] = scales[j];
+        // insertion sort (stable) with isless ordering
+        for (int i = 1; i < m; ++i) {
+            double key = arr[i];
+            int q = i - 1;
+            while (q >= 0 && jisless(key, arr[q])) { arr[q + 1] = arr[q]; --q; }
+            arr[q + 1] = key;
+        }
+        double prod = 1.0;
+        bool ok;
+        if (SEL == 2) {
+            // binary16 evaluation: products of two binary16 values are exact
+            // in binary32, so one rounding to binary16 per step reproduces
+            // native half arithmetic.
+            float ph = 1.0f;
+            for (int i = 0; i < m / 2; ++i) {
+                prod *= arr[i] * arr[m - 1 - i];
+                float a = __half2float(__double2half(arr[i])), b = __half2float(__double2half(arr[m - 1 - i]));
+                float pair = __half2float(__float2half_rn(a * b));
+                ph = __half2float(__float2half_rn(ph * pair));
+            }
+            if (m & 1) {
+                prod *= arr[m / 2];
+                float a = __half2float(__double2half(arr[m / 2]));
+                ph = __half2float(__float2half_rn(ph * a));
+            }
+            ok = sel_finite_half(ph);
+        } else if (SEL == 1) {
+            float pf = 1.0f;
+            for (int i = 0; i < m / 2; ++i) {
+                prod *= arr[i] * arr[m - 1 - i];
+                pf = pf * ((float)arr[i] * (float)arr[m - 1 - i]);
+            }
+            if (m & 1) {
+                prod *= arr[m / 2];
+                pf = pf * (float)arr[m / 2];
+            }
+            ok = isfinite(pf);
+        } else {
+            for (int i = 0; i < m / 2; ++i) prod *= arr[i] * arr[m - 1 - i];
+            if (m & 1) prod *= arr[m / 2];
+            ok = true;
+        }
+        if (ok && isfinite(prod)) {
+            *jout = j;
+            return prod;
+        }
+    }
+    *jout = -1;
+    return 0.0;
+}
+
+// ------------------------------------------------- fixed-point tallies
+// Signed 3-limb fixed point: V = round_half_up(v * 2^-b) with |V| < 2^94,
+// limbs of weight 2^64, 2^32 and 1 held in separate int64 accumulators.  Each
+// accumulator holds the exact signed sum of its limbs (|sum| < n * 2^32 for n
+// additions, far below 2^63), so the recombined total is exact whatever the
+// order of additions.  The conversion is pure integer arithmetic: no FP64 on
+// the FP32 hot path.
+struct Limbs { long long l0, l1, l2; };
+
+IMC_HD uint32_t f2u(float v) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(v);
+#else
+    uint32_t u; memcpy(&u, &v, 4); return u;
+#endif
+}
+IMC_HD uint64_t d2u(double v) {
+#ifdef __CUDA_ARCH__
+    return (uint64_t)__double_as_longlong(v);
+#else
+    uint64_t u; memcpy(&u, &v, 8); return u;
+#endif
+}
+IMC_HD int bitlen64(uint64_t m) {
+#ifdef __CUDA_ARCH__
+    return 64 - __clzll((long long)m);
+#else
+    return m ? 64 - __builtin_clzll(m) : 0;
+#endif
+}
+
+// man * 2^sh (man < 2^53), rounded half-up, signed; false if |V| >= 2^94
+IMC_HD bool fix_place(uint64_t man, int sh, bool neg, Limbs &o) {
+    uint64_t lo = 0, hi = 0;
+    if (man == 0) { o.l0 = o.l1 = o.l2 = 0; return true; }
+    if (sh >= 0) {
+        if (bitlen64(man) + sh > 94) return false;
+        if (sh == 0) { lo = man; hi = 0; }
+        else if (sh < 64) { lo = man << sh; hi = man >> (64 - sh); }
+        else { lo = 0; hi = man << (sh - 64); }
+    } else {
+        int r = -sh;
+        if (r >= 60) { lo = 0; }
+        else { lo = (man + (1ull << (r - 1))) >> r; }
+        hi = 0;
+    }
+    long long l2 = (long long)(lo & 0xFFFFFFFFull);
+    long long l1 = (long long)(lo >> 32);
+    long long l0 = (long long)hi;
+    if (neg) { l0 = -l0; l1 = -l1; l2 = -l2; }
+    o.l0 = l0; o.l1 = l1; o.l2 = l2;
+    return true;
+}
+
+IMC_HD bool fix_split(float v, int b, Limbs &o) {
+    uint32_t bits = f2u(v);
+    bool neg = (bits >> 31) != 0;
+    int ex = (int)((bits >> 23) & 0xFFu);
+    if (ex == 0xFF) return false;
+    uint64_t man = bits & 0x7FFFFFu;
+    int e2;
+    if (ex == 0) e2 = 1 - 127 - 23;
+    else { man |= 0x800000u; e2 = ex - 127 - 23; }
+    return fix_place(man, e2 - b, neg, o);
+}
+IMC_HD bool fix_split(double v, int b, Limbs &o) {
+    uint64_t bits = d2u(v);
+    bool neg = (bits >> 63) != 0;
+    int ex = (int)((bits >> 52) & 0x7FFu);
+    if (ex == 0x7FF) return false;
+    uint64_t man = bits & 0xFFFFFFFFFFFFFull;
+    int e2;
+    if (ex == 0) e2 = 1 - 1023 - 52;
+    else { man |= 0x10000000000000ull; e2 = ex - 1023 - 52; }
+    return fix_place(man, e2 - b, neg, o);
+}
+
+// Exponent b with every |v| <= vmax mapping below 2^93 (one spare bit for a
+// value a rounding step above vmax, one for the compensation term).
+IMC_HD int fix_exponent(double vmax) {
+    if (!(vmax > 0.0) || !(vmax < 1.0e308)) return -1074;
+    int e = ilogb(vmax);
+    return e + 1 - 93;
+}
+
+// signed total of accumulator words a[0..2] times 2^b
+IMC_HD double fix_value(const long long *a, int b) {
+    uint64_t hi = (uint64_t)a[0], lo = 0;
+    // + a1 * 2^32 (sign-extended)
+    uint64_t lo1 = (uint64_t)a[1] << 32;
+    uint64_t hi1 = (uint64_t)(a[1] >> 32);
+    lo += lo1;
+    hi += hi1 + (lo < lo1 ? 1ull : 0ull);
+    // + a2 (sign-extended)
+    uint64_t lo2 = (uint64_t)a[2];
+    uint64_t hi2 = a[2] < 0 ? ~0ull : 0ull;
+    uint64_t plo = lo;
+    lo += lo2;
+    hi += hi2 + (lo < plo ? 1ull : 0ull);
+    double v = (double)(long long)hi * 0x1p64 + (double)lo;
+    return scalbn(v, b);
+}
+
+// ------------------------------------------------ double-double summation
+// no constructor, so arrays of DD may live in __shared__ memory
+struct DD {
+    double hi, lo;
+    IMC_HD void clear() { hi = 0.0; lo = 0.0; }
+    IMC_HD void add(double x) {
+        double s = hi + x;
+        double bp = s - hi;
+        double e = (hi - (s - bp)) + (x - bp);
+        hi = s;
+        lo += e;
+    }
+    IMC_HD void add(const DD &o) {
+        add(o.hi);
+        lo += o.lo;
+    }
+    IMC_HD double val() const { return hi + lo; }
+};
+
+}  // namespace imc

@@ -1,0 +1,97 @@
+// imc_internal.h -- device data layout and kernel launchers shared by the
+// translation units of libimc.so.  Not part of the public ABI (include/imc.h).
+//
+// Layout in HBM
+//   cell state      FP64 arrays of ncells (temp, bee, beta, fleck, sigma_a,
+//                   sigma_s, matenergydens, radenergydens) and ncells*K
+//                   (energydep, emittedenergy), K = number of energy scales.
+//   particles       two ping-pong structure-of-arrays buffers; one field per
+//                   array so every load and store is coalesced:
+//                     1D: t, x, mu, E, E0, cs      2D: t, x, y, ux, uy, E, E0, cs
+//                   FP64 / FP32 store physical values; FP16 stores x/(dx*ds),
+//                   y/(dy*ds), t/dt, E/E0 and the direction in binary16 with E0
+//                   in binary32.  cs = cell | scale_index << 24.  alive is one
+//                   byte per particle.
+//   tallies         3-limb fixed-point accumulators (int64) per (scale, cell)
+//                   for deposition and census energy, per scale for escaped
+//                   energy; finalised to FP64 by the tally kernel.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+
+namespace imc {
+
+// scalars that live in device memory so a whole step can replay as a graph
+struct Scalars {
+    double t, dt;
+    double totalenergy, totalenergydep, lostenergy, radenergyold, radenergy, energy_err;
+    double lost_step;                  // escaped energy of this step
+    unsigned long long emax_census_bits;  // max census energy (bits of a non-negative double)
+    double emax;                       // max particle energy at transport start
+    long long n_census;                // census (after clean); start of the list
+    long long n_census_in;             // census carried into this step
+    long long n_particles;             // list length after sourcing
+    long long n_sourced;
+    unsigned long long segments;
+    unsigned long long surrogate_calls;
+    unsigned int flags;
+    int b_dep, b_rad, b_lost;          // fixed-point exponents of this transport
+    unsigned int step;                 // step index (RNG key, stats slot)
+    int finished;                      // t > t_end
+    int pad;
+};
+
+struct CellArgs {
+    int geometry, nx, ny, nc, K;
+    const double *dx, *dy;
+    double *temp, *bee, *beta, *fleck, *sa, *ss;
+    const double *sa_val, *sa_pow, *ss_val, *ss_pow, *radsource, *tsurf, *scales;
+    double *energydep, *emitted, *radenergydens, *matenergydens;
+    long long *dep_acc, *rad_acc, *lost_acc;   // 3 limbs per slot
+    // sourcing scratch (per source slot)
+    int nslots;
+    double *slot_e, *slot_s, *slot_nrg;
+    int *slot_j;
+    long long *slot_n, *slot_off;
+    // physics / control
+    int bc[4];
+    double c, a, alpha, ds, temp_floor, cellmin;
+    int linearized, marshak, sel_prec, timestepping;
+    long long n_input, n_max, capacity, seg_cap;
+    unsigned long long seed;
+    double vol_min, scale_min;
+    double t_end, dtmax, kfac;
+};
+
+// type-erased particle buffer
+struct PBufRaw {
+    void *t, *x, *y, *ux, *uy, *E, *E0;
+    int32_t *cs;
+    uint8_t *alive;
+};
+
+// per-step statistics slot written on the device
+struct DevStats {
+    double t, dt, total_energy, energy_dep, rad_energy, rad_energy_old, lost_energy, energy_error;
+    long long n_census_in, n_sourced, n_census_out, segments, surrogate_calls;
+    unsigned int error_flags, step_index;
+};
+
+// launchers (imc_kernels.cu / imc_transport.cu); all asynchronous on `st`
+void launch_update(const CellArgs &ca, Scalars *sc, cudaStream_t st);
+void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, cudaStream_t st);
+void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, int block, cudaStream_t st);
+void launch_compact(const CellArgs &ca, Scalars *sc, int prec, PBufRaw src, PBufRaw dst, long long *tile_cnt,
+                    long long *tile_off, long long ntiles_cap, cudaStream_t st);
+void launch_tally(const CellArgs &ca, Scalars *sc, cudaStream_t st);
+void launch_energycheck(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap, cudaStream_t st);
+void launch_timestep(const CellArgs &ca, Scalars *sc, cudaStream_t st);
+void launch_prepare_transport(const CellArgs &ca, Scalars *sc, cudaStream_t st);
+int transport_smem_bytes(const CellArgs &ca, int prec);
+const void *transport_kernel_ptr(const CellArgs &ca, int prec);
+
+constexpr int kCompactTile = 4096;     // particles per compaction tile
+constexpr int kCompactThreads = 256;
+
+}  // namespace imc

@@ -1,0 +1,699 @@
+// imc_kernels.cu -- the O(ncells) stages (FP64) and the particle-list stages
+// around transport.
+//
+//   k_update           <- Update.update                 src/imc_update.jl:12-56
+//   k_source_slots     <- Sourcing.sourcing, energies     src/imc_sourcing.jl:56-121
+//   k_source_plan      <- Sourcing.sourcing, budget/counts src/imc_sourcing.jl:121-157
+//   k_source_emit      <- Sourcing.sourcing, births        src/imc_sourcing.jl:159-366
+//   k_compact_*        <- Clean.clean                    src/imc_clean.jl:6-19
+//   k_tally            <- Tally.tally                    src/imc_tally.jl:22-142
+//   k_energycheck      <- EnergyCheck.energychecker      src/imc_energycheck.jl:19-38
+//   k_timestep         <- timestep                       src/MixedPrecisionIMC.jl:181-222
+//
+// Sums over cells are double-double per thread over a fixed assignment of
+// elements, then a fixed-order tree: deterministic, and within a rounding of
+// the exact sum.  Every launch has a fixed grid and reads its sizes from
+// device scalars, so a whole step can be captured once as a CUDA graph.
+#include <cstdint>
+#include "imc_device.cuh"
+#include "imc_internal.h"
+#include "imc_state.cuh"
+
+namespace imc {
+
+constexpr int kPlanThreads = 1024;
+
+// ------------------------------------------------------------------ update
+__global__ void k_update(CellArgs ca, Scalars *sc) {
+    const double a = ca.a, c = ca.c, dt = sc->dt;
+    const double one[1] = {1.0};
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->flags = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ca.nc; i += gridDim.x * blockDim.x) {
+        double T = ca.temp[i];
+        double T3 = T * T * T;
+        double beta;
+        if (ca.linearized) {
+            ca.bee[i] = (4.0 * a) * T3;
+            beta = 1.0;
+        } else {
+            beta = ((4.0 * a) * T3) / ca.bee[i];
+        }
+        ca.beta[i] = beta;
+        double Tc = (ca.temp_floor > 0.0 && T < ca.temp_floor) ? ca.temp_floor : T;
+        double sa = ca.sa_val[i] * pow(Tc, ca.sa_pow[i]);
+        if (ca.marshak) sa = ca.sa_val[i] / Tc / Tc / Tc;
+        ca.sa[i] = sa;
+        ca.ss[i] = ca.ss_val[i] * pow(Tc, ca.ss_pow[i]);
+        double v[6] = {ca.ds, ca.alpha, beta, c, dt, sa};
+        int j;
+        double prod = sorter<0>(v, 6, one, 1, &j);
+        ca.fleck[i] = 1.0 / (1.0 + prod);
+    }
+}
+
+void launch_update(const CellArgs &ca, Scalars *sc, cudaStream_t st) {
+    int grid = (ca.nc + 255) / 256;
+    if (grid > 1024) grid = 1024;
+    k_update<<<grid, 256, 0, st>>>(ca, sc);
+}
+
+// ---------------------------------------------------------------- sourcing
+__device__ __forceinline__ double sorter_sel(int sel, const double *v, int n, const double *sc, int K, int *j) {
+    if (sel == 2) return sorter<2>(v, n, sc, K, j);
+    if (sel == 1) return sorter<1>(v, n, sc, K, j);
+    return sorter<0>(v, n, sc, K, j);
+}
+
+__device__ __forceinline__ int nsurf_slots(const CellArgs &ca) {
+    return ca.geometry == 1 ? 2 : 2 * ca.nx + 2 * ca.ny;
+}
+
+// Energies per source slot.  Slot order is the reference's push! order:
+// 1D [left, right, body cells, source cells]; 2D [bottom x, top x, left y,
+// right y, body cells, source cells].
+__global__ void k_source_slots(CellArgs ca, Scalars *sc) {
+    const double a = ca.a, c = ca.c, ds = ca.ds, dt = sc->dt;
+    const int ns = nsurf_slots(ca), nc = ca.nc, K = ca.K;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ca.nslots; s += gridDim.x * blockDim.x) {
+        double e = 0.0;
+        int j = -1;
+        if (s < ns) {
+            double Ts, w = 0.0;
+            int nv;
+            double v[9];
+            if (ca.geometry == 1) {
+                Ts = ca.tsurf[s];
+                double vv[8] = {a, c, Ts, Ts, Ts, Ts, dt, 0.25};
+                for (int q = 0; q < 8; ++q) v[q] = vv[q];
+                nv = 8;
+            } else {
+                Ts = ca.tsurf[s];
+                if (s < 2 * ca.nx) w = ca.dx[s % ca.nx];
+                else w = ca.dy[(s - 2 * ca.nx) % ca.ny];
+                double vv[9] = {a, c, Ts, Ts, Ts, Ts, w, dt, 0.25};
+                for (int q = 0; q < 9; ++q) v[q] = vv[q];
+                nv = 9;
+            }
+            e = sorter_sel(ca.sel_prec, v, nv, ca.scales, K, &j);
+        } else if (s < ns + nc) {
+            const int i = s - ns;
+            const int ix = ca.geometry == 1 ? i : i % ca.nx;
+            const int iy = ca.geometry == 1 ? 0 : i / ca.nx;
+            const double T = ca.temp[i], f = ca.fleck[i], sa = ca.sa[i];
+            if (ca.geometry == 1) {
+                double v[11] = {f, sa, a, c, T, T, T, T, ca.dx[i], dt, ds};
+                e = sorter_sel(ca.sel_prec, v, 11, ca.scales, K, &j);
+            } else {
+                double v[12] = {f, sa, a, c, T, T, T, T, ca.dx[ix], ca.dy[iy], dt, ds};
+                e = sorter_sel(ca.sel_prec, v, 12, ca.scales, K, &j);
+            }
+            // emitted energy density (src/imc_sourcing.jl:69-70)
+            double ve[10] = {f, sa, a, c, T, T, T, T, dt, ds};
+            int je;
+            double em = sorter_sel(ca.sel_prec, ve, 10, ca.scales, K, &je);
+            for (int q = 0; q < K; ++q) ca.emitted[(size_t)q * nc + i] = 0.0;
+            if (je >= 0) ca.emitted[(size_t)je * nc + i] = em;
+            else atomicOr(&sc->flags, 1u << 5);
+        } else {
+            const int i = s - ns - nc;
+            const int ix = ca.geometry == 1 ? i : i % ca.nx;
+            const int iy = ca.geometry == 1 ? 0 : i / ca.nx;
+            if (ca.geometry == 1) {
+                double v[3] = {ca.radsource[i], ca.dx[i], dt};
+                e = sorter_sel(ca.sel_prec, v, 3, ca.scales, K, &j);
+            } else {
+                double v[4] = {ca.radsource[i], ca.dx[ix], ca.dy[iy], dt};
+                e = sorter_sel(ca.sel_prec, v, 4, ca.scales, K, &j);
+            }
+        }
+        if (j < 0) atomicOr(&sc->flags, 1u << 5);
+        ca.slot_e[s] = e;
+        ca.slot_s[s] = j >= 0 ? ca.scales[j] : 0.0;
+        ca.slot_j[s] = j;
+    }
+}
+
+// deterministic block-wide double-double sum (one block)
+template <class F> __device__ double block_dd_sum(int n, F f, DD *sh) {
+    DD d;
+    d.clear();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) d.add(f(i));
+    sh[threadIdx.x] = d;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            DD x = sh[threadIdx.x];
+            x.add(sh[threadIdx.x + w]);
+            sh[threadIdx.x] = x;
+        }
+        __syncthreads();
+    }
+    double r = sh[0].val();
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ long long round_count(double e, double s, double n_source, double E, bool withmin,
+                                                 double cellmin) {
+    double r = rint(((e / s) * n_source) / E);
+    if (withmin) r = fmax(r, cellmin);
+    return (long long)r;
+}
+
+// Budget, per-slot counts and energies, exclusive scan, fixed-point exponents.
+__global__ void __launch_bounds__(kPlanThreads) k_source_plan(CellArgs ca, Scalars *sc) {
+    __shared__ DD sh[kPlanThreads];
+    __shared__ long long warp_tot[32];
+    __shared__ long long s_run;
+    __shared__ double s_emax;
+    const int ns = nsurf_slots(ca), nc = ca.nc;
+    const double *e = ca.slot_e, *s = ca.slot_s;
+    double body = block_dd_sum(nc, [&](int i) { return e[ns + i] / s[ns + i]; }, sh);
+    double rad = block_dd_sum(nc, [&](int i) { return e[ns + nc + i] / s[ns + nc + i]; }, sh);
+    double e_surface;
+    if (ca.geometry == 1) {
+        e_surface = (e[0] / s[0]) + (e[1] / s[1]);
+    } else {
+        const int nx = ca.nx, ny = ca.ny;
+        e_surface = 0.0;
+        e_surface += block_dd_sum(nx, [&](int i) { return e[i] / s[i]; }, sh);
+        e_surface += block_dd_sum(nx, [&](int i) { return e[nx + i] / s[nx + i]; }, sh);
+        e_surface += block_dd_sum(ny, [&](int i) { return e[2 * nx + i] / s[2 * nx + i]; }, sh);
+        e_surface += block_dd_sum(ny, [&](int i) { return e[2 * nx + ny + i] / s[2 * nx + ny + i]; }, sh);
+    }
+    const double E = body + rad + e_surface;
+    const long long n_census = sc->n_census;
+    double n_source = (double)ca.n_input;
+    if (ca.n_input + n_census > ca.n_max) {
+        double lenN = ca.geometry == 1 ? 1.0 : 2.0;
+        n_source = fmax(ca.cellmin, (double)(ca.n_max - n_census) - lenN - 1.0);
+    }
+    const bool ok = (E > 0.0) && isfinite(E);
+    const bool surf_min = ca.geometry == 2;
+    // counts and per-particle energies
+    for (int q = threadIdx.x; q < ca.nslots; q += blockDim.x) {
+        long long n = 0;
+        if (ok) {
+            if (q < ns) {
+                if (e[q] > 0) n = round_count(e[q], s[q], n_source, E, surf_min, ca.cellmin);
+            } else if (q < ns + nc) {
+                n = round_count(e[q], s[q], n_source, E, true, ca.cellmin);
+            } else {
+                if (e[q] > 0) {
+                    n = round_count(e[q], s[q], n_source, E, true, ca.cellmin);
+                    // 2D births n_body particles per source cell (src/imc_sourcing.jl:357)
+                    if (ca.geometry == 2 && n > 0)
+                        n = round_count(e[q - nc], s[q - nc], n_source, E, true, ca.cellmin);
+                }
+            }
+            if (n < 0) n = 0;
+        }
+        double nrg = 0.0;
+        if (n > 0) {
+            long long nd = n;
+            if (ca.geometry == 2 && q >= ns + nc) nd = round_count(e[q], s[q], n_source, E, true, ca.cellmin);
+            nrg = e[q] / (double)nd;
+        }
+        ca.slot_n[q] = n;
+        ca.slot_nrg[q] = nrg;
+    }
+    if (threadIdx.x == 0) { s_run = 0; s_emax = 0.0; }
+    __syncthreads();
+    // exclusive scan of slot_n, chunked
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int base = 0; base < ca.nslots; base += blockDim.x) {
+        int q = base + threadIdx.x;
+        long long v = q < ca.nslots ? ca.slot_n[q] : 0;
+        long long x = v;
+        for (int off = 1; off < 32; off <<= 1) {
+            long long y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+            if (lane >= off) x += y;
+        }
+        if (lane == 31) warp_tot[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            long long w = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+            for (int off = 1; off < 32; off <<= 1) {
+                long long y = __shfl_up_sync(0xFFFFFFFFu, w, off);
+                if (lane >= off) w += y;
+            }
+            warp_tot[lane] = w;
+        }
+        __syncthreads();
+        long long excl = s_run + (warp > 0 ? warp_tot[warp - 1] : 0) + x - v;
+        if (q < ca.nslots) ca.slot_off[q] = excl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) s_run = excl + v;
+        __syncthreads();
+    }
+    // largest per-particle energy of this step's births
+    double my = 0.0;
+    for (int q = threadIdx.x; q < ca.nslots; q += blockDim.x)
+        if (ca.slot_n[q] > 0 && ca.slot_nrg[q] > my) my = ca.slot_nrg[q];
+    for (int off = 16; off > 0; off >>= 1) {
+        double o = __shfl_down_sync(0xFFFFFFFFu, my, off);
+        my = o > my ? o : my;
+    }
+    if (lane == 0) {
+        unsigned long long bits = (unsigned long long)d2u(my);
+        atomicMax((unsigned long long *)&s_emax, bits);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long n_new = s_run;
+        unsigned fl = 0;
+        if (!ok) fl |= 1u << 4;
+        if (n_census + n_new > ca.capacity) {
+            n_new = ca.capacity - n_census;
+            if (n_new < 0) n_new = 0;
+            fl |= 1u << 3;
+        }
+        double emax_c = __longlong_as_double((long long)sc->emax_census_bits);
+        double emax = fmax(emax_c, s_emax);
+        sc->totalenergy = E;
+        sc->n_census_in = n_census;
+        sc->n_sourced = n_new;
+        sc->n_particles = n_census + n_new;
+        sc->emax = emax;
+        sc->emax_census_bits = 0ull;
+        sc->segments = 0ull;
+        sc->surrogate_calls = 0ull;
+        sc->b_dep = fix_exponent(emax / ca.vol_min);
+        sc->b_lost = fix_exponent(emax);
+        sc->b_rad = fix_exponent(emax);
+        if (fl) sc->flags |= fl;
+    }
+}
+
+template <class T> struct RT;
+template <> struct RT<float> { static __device__ float sqrt_(float x) { return sqrtf(x); } };
+template <> struct RT<double> { static __device__ double sqrt_(double x) { return sqrt(x); } };
+
+template <class St>
+__device__ __forceinline__ void store_birth(const CellArgs &ca, PBuf<St> &pb, long long pid, typename St::T t,
+                                            typename St::T x, typename St::T y, typename St::T ux,
+                                            typename St::T uy, typename St::T E0, int cell, int k, float dtf) {
+    typedef typename St::S S;
+    if (St::half) {
+        const int ix = ca.geometry == 1 ? cell : cell % ca.nx;
+        float dxs = (float)ca.dx[ix] * (float)ca.ds;
+        st_v(pb.x + pid, (float)x / dxs);
+        if (ca.geometry == 2) {
+            const int iy = cell / ca.nx;
+            float dys = (float)ca.dy[iy] * (float)ca.ds;
+            st_v(pb.y + pid, (float)y / dys);
+            st_v(pb.uy + pid, (float)uy);
+        }
+        st_v(pb.t + pid, (float)t / dtf);
+        st_v(pb.ux + pid, (float)ux);
+        st_v(pb.E + pid, 1.0f);
+        pb.E0[pid] = (float)E0;
+    } else {
+        pb.t[pid] = (S)t;
+        pb.x[pid] = (S)x;
+        pb.ux[pid] = (S)ux;
+        if (ca.geometry == 2) { pb.y[pid] = (S)y; pb.uy[pid] = (S)uy; }
+        pb.E[pid] = (S)E0;
+        pb.E0[pid] = (typename St::E0S)E0;
+    }
+    pb.cs[pid] = cell | (k << 24);
+    pb.alive[pid] = 1;
+}
+
+// One thread per newborn particle; its stream is keyed by its list index.
+template <class St>
+__global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, PBufRaw raw) {
+    typedef typename St::T T;
+    PBuf<St> pb(raw);
+    const long long n_new = sc->n_sourced, n_census = sc->n_census_in;
+    const unsigned step = sc->step;
+    const double dtd = sc->dt;
+    const T dtT = (T)dtd, dsT = (T)ca.ds;
+    const int ns = nsurf_slots(ca), nc = ca.nc, nslots = ca.nslots;
+    const double pd = 3.141592653589793;
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n_new;
+         j += (long long)gridDim.x * blockDim.x) {
+        // slot = last q with slot_off[q] <= j
+        int lo = 0, hi = nslots;
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (ca.slot_off[mid] <= j) lo = mid;
+            else hi = mid;
+        }
+        const int q = lo;
+        const long long pid = n_census + j;
+        Stream rs;
+        rs.init(ca.seed, step, (uint32_t)pid, kStageSource);
+        const T E0 = (T)ca.slot_nrg[q];
+        const int k = ca.slot_j[q] < 0 ? 0 : ca.slot_j[q];
+        if (ca.geometry == 1) {
+            if (q < 2) {
+                // surface births (src/imc_sourcing.jl:161-189)
+                const int cell = q == 0 ? 0 : ca.nx - 1;
+                const double frac = q == 0 ? 0.01 : 0.99;
+                T xpos = (T)(frac * (double)(T)ca.dx[cell] * (double)dsT);
+                T mu = (T)0;
+                for (int r = 0; r < 64 && mu == (T)0; ++r) {
+                    T rr = RT<T>::sqrt_(Rand<T>::u(rs));
+                    mu = q == 0 ? rr : -rr;
+                }
+                if (mu == (T)0) mu = q == 0 ? (T)1 : (T)-1;
+                T st = dtT * Rand<T>::u(rs);
+                store_birth<St>(ca, pb, pid, st, xpos, (T)0, mu, (T)0, E0, cell, k, (float)dtT);
+            } else {
+                // body / source births (src/imc_sourcing.jl:193-236)
+                const int cell = q < ns + nc ? q - ns : q - ns - nc;
+                T xpos = (T)ca.dx[cell] * Rand<T>::u(rs) * dsT;
+                T mu = (T)0;
+                for (int r = 0; r < 64 && mu == (T)0; ++r) mu = (T)1 - (T)2 * Rand<T>::u(rs);
+                if (mu == (T)0) mu = (T)1;
+                T st = dtT * Rand<T>::u(rs);
+                store_birth<St>(ca, pb, pid, st, xpos, (T)0, mu, (T)0, E0, cell, k, (float)dtT);
+            }
+        } else {
+            T st, xpos, ypos, ang;
+            int ix, iy;
+            if (q < ns) {
+                // surface births (src/imc_sourcing.jl:265-323)
+                const int nx = ca.nx, ny = ca.ny;
+                int face, idx;
+                if (q < nx) { face = 0; idx = q; }
+                else if (q < 2 * nx) { face = 1; idx = q - nx; }
+                else if (q < 2 * nx + ny) { face = 2; idx = q - 2 * nx; }
+                else { face = 3; idx = q - 2 * nx - ny; }
+                st = dtT * Rand<T>::u(rs);
+                if (face < 2) {
+                    ix = idx;
+                    iy = face == 0 ? 0 : ny - 1;
+                    xpos = (T)ca.dx[ix] * Rand<T>::u(rs) * dsT;
+                    ypos = face == 0 ? (T)(0.001 * (double)(T)ca.dy[0] * (double)dsT)
+                                     : (T)(0.999 * (double)(T)ca.dy[ny - 1] * (double)dsT);
+                    T u = Rand<T>::u(rs);
+                    ang = face == 0 ? (T)((T)pd * u) : (T)(-pd * (double)u);
+                } else {
+                    iy = idx;
+                    ix = face == 2 ? 0 : nx - 1;
+                    xpos = face == 2 ? (T)(0.001 * (double)(T)ca.dx[0] * (double)dsT)
+                                     : (T)(0.999 * (double)(T)ca.dx[nx - 1] * (double)dsT);
+                    // the reference scales y by mesh.dx[j] (src/imc_sourcing.jl:301,316)
+                    const double wq = iy < nx ? ca.dx[iy] : ca.dy[iy];
+                    ypos = (T)wq * Rand<T>::u(rs) * dsT;
+                    T u = Rand<T>::u(rs);
+                    ang = face == 2 ? (T)(pd * (0.5 - (double)u)) : (T)(pd * (0.5 + (double)u));
+                }
+            } else {
+                // body / source births (src/imc_sourcing.jl:326-366)
+                const int cell = q < ns + nc ? q - ns : q - ns - nc;
+                ix = cell % ca.nx;
+                iy = cell / ca.nx;
+                xpos = (T)ca.dx[ix] * Rand<T>::u(rs) * dsT;
+                ypos = (T)ca.dy[iy] * Rand<T>::u(rs) * dsT;
+                ang = (T)(2.0 * pd * (double)Rand<T>::u(rs));
+                st = dtT * Rand<T>::u(rs);
+            }
+            T ux, uy;
+            if (sizeof(T) == 4) { float s_, c_; sincosf((float)ang, &s_, &c_); ux = (T)c_; uy = (T)s_; }
+            else { double s_, c_; sincos((double)ang, &s_, &c_); ux = (T)c_; uy = (T)s_; }
+            store_birth<St>(ca, pb, pid, st, xpos, ypos, ux, uy, E0, ix + iy * ca.nx, k, (float)dtT);
+        }
+    }
+}
+
+void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, cudaStream_t st) {
+    int g = (ca.nslots + 255) / 256;
+    if (g > 1024) g = 1024;
+    k_source_slots<<<g, 256, 0, st>>>(ca, sc);
+    k_source_plan<<<1, kPlanThreads, 0, st>>>(ca, sc);
+    if (prec == 0) k_source_emit<StF64><<<grid, 256, 0, st>>>(ca, sc, buf);
+    else if (prec == 1) k_source_emit<StF32><<<grid, 256, 0, st>>>(ca, sc, buf);
+    else k_source_emit<StF16><<<grid, 256, 0, st>>>(ca, sc, buf);
+}
+
+// ------------------------------------------------------------- compaction
+// Stable three-pass compaction: per-tile alive counts, one-block exclusive
+// scan of the tile counts, then a per-tile block scan that scatters the
+// survivors in order into the other buffer.
+__global__ void __launch_bounds__(kCompactThreads) k_compact_count(const Scalars *sc, const uint8_t *alive,
+                                                                   long long *tile_cnt) {
+    const long long n = sc->n_particles;
+    const long long base = (long long)blockIdx.x * kCompactTile;
+    if (base >= n) return;
+    int cnt = 0;
+    for (int r = threadIdx.x; r < kCompactTile; r += blockDim.x) {
+        long long i = base + r;
+        if (i < n && alive[i]) ++cnt;
+    }
+    cnt = __reduce_add_sync(0xFFFFFFFFu, (unsigned)cnt);
+    __shared__ int wt[kCompactThreads / 32];
+    if ((threadIdx.x & 31) == 0) wt[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long s = 0;
+        for (int w = 0; w < kCompactThreads / 32; ++w) s += wt[w];
+        tile_cnt[blockIdx.x] = s;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_compact_scan(Scalars *sc, const long long *tile_cnt, long long *tile_off) {
+    __shared__ long long warp_tot[32];
+    __shared__ long long s_run;
+    const long long n = sc->n_particles;
+    const long long ntiles = (n + kCompactTile - 1) / kCompactTile;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_run = 0;
+    __syncthreads();
+    for (long long base = 0; base < ntiles; base += blockDim.x) {
+        long long q = base + threadIdx.x;
+        long long v = q < ntiles ? tile_cnt[q] : 0;
+        long long x = v;
+        for (int off = 1; off < 32; off <<= 1) {
+            long long y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+            if (lane >= off) x += y;
+        }
+        if (lane == 31) warp_tot[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            long long w = warp_tot[lane];
+            for (int off = 1; off < 32; off <<= 1) {
+                long long y = __shfl_up_sync(0xFFFFFFFFu, w, off);
+                if (lane >= off) w += y;
+            }
+            warp_tot[lane] = w;
+        }
+        __syncthreads();
+        long long excl = s_run + (warp > 0 ? warp_tot[warp - 1] : 0) + x - v;
+        if (q < ntiles) tile_off[q] = excl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) s_run = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        sc->n_census = s_run;
+        sc->n_particles = s_run;
+    }
+}
+
+template <class St>
+__global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(int geometry, const Scalars *sc,
+                                                                     const long long *tile_off, PBufRaw sraw,
+                                                                     PBufRaw draw, const long long *n_before) {
+    PBuf<St> src(sraw), dst(draw);
+    const long long n = *n_before;
+    const long long base = (long long)blockIdx.x * kCompactTile;
+    if (base >= n) return;
+    __shared__ int wt[kCompactThreads / 32];
+    __shared__ int s_tot;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    long long run = tile_off[blockIdx.x];
+    for (int r = 0; r < kCompactTile; r += kCompactThreads) {
+        const long long i = base + r + threadIdx.x;
+        const bool f = i < n && src.alive[i];
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, f);
+        const int wpre = __popc(m & ((1u << lane) - 1u));
+        if (lane == 0) wt[warp] = __popc(m);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int s = 0;
+            for (int w = 0; w < kCompactThreads / 32; ++w) { int v = wt[w]; wt[w] = s; s += v; }
+            s_tot = s;
+        }
+        __syncthreads();
+        if (f) {
+            const long long d = run + wt[warp] + wpre;
+            dst.t[d] = src.t[i];
+            dst.x[d] = src.x[i];
+            dst.ux[d] = src.ux[i];
+            if (geometry == 2) { dst.y[d] = src.y[i]; dst.uy[d] = src.uy[i]; }
+            dst.E[d] = src.E[i];
+            dst.E0[d] = src.E0[i];
+            dst.cs[d] = src.cs[i];
+            dst.alive[d] = 1;
+        }
+        run += s_tot;
+        __syncthreads();
+    }
+}
+
+__global__ void k_copy_count(const Scalars *sc, long long *n_before) { *n_before = sc->n_particles; }
+
+void launch_compact(const CellArgs &ca, Scalars *sc, int prec, PBufRaw src, PBufRaw dst, long long *tile_cnt,
+                    long long *tile_off, long long ntiles_cap, cudaStream_t st) {
+    // tile_off has ntiles_cap + 1 entries; the last holds the pre-compaction length
+    long long *n_before = tile_off + ntiles_cap;
+    k_copy_count<<<1, 1, 0, st>>>(sc, n_before);
+    k_compact_count<<<(unsigned)ntiles_cap, kCompactThreads, 0, st>>>(sc, src.alive, tile_cnt);
+    k_compact_scan<<<1, 1024, 0, st>>>(sc, tile_cnt, tile_off);
+    if (prec == 0)
+        k_compact_scatter<StF64><<<(unsigned)ntiles_cap, kCompactThreads, 0, st>>>(ca.geometry, sc, tile_off, src, dst, n_before);
+    else if (prec == 1)
+        k_compact_scatter<StF32><<<(unsigned)ntiles_cap, kCompactThreads, 0, st>>>(ca.geometry, sc, tile_off, src, dst, n_before);
+    else
+        k_compact_scatter<StF16><<<(unsigned)ntiles_cap, kCompactThreads, 0, st>>>(ca.geometry, sc, tile_off, src, dst, n_before);
+}
+
+// ------------------------------------------------------------------- tally
+__device__ __forceinline__ double cell_vol(const CellArgs &ca, int i) {
+    return ca.geometry == 1 ? ca.dx[i] : ca.dx[i % ca.nx] * ca.dy[i / ca.nx];
+}
+
+__global__ void __launch_bounds__(kPlanThreads) k_tally(CellArgs ca, Scalars *sc) {
+    __shared__ DD sh[kPlanThreads];
+    const int nc = ca.nc, K = ca.K;
+    const int b_dep = sc->b_dep, b_rad = sc->b_rad, b_lost = sc->b_lost;
+    // finalise the fixed-point tallies of this step's transport
+    for (int idx = threadIdx.x; idx < K * nc; idx += blockDim.x) {
+        long long *d = ca.dep_acc + 3 * (size_t)idx;
+        ca.energydep[idx] = fix_value(d, b_dep);
+        d[0] = d[1] = d[2] = 0;
+    }
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+        const double vol = cell_vol(ca, i);
+        double r = 0.0;
+        for (int k = 0; k < K; ++k) {
+            long long *d = ca.rad_acc + 3 * ((size_t)k * nc + i);
+            r += fix_value(d, b_rad) / (vol * ca.scales[k]);
+            d[0] = d[1] = d[2] = 0;
+        }
+        ca.radenergydens[i] = r;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double lost = 0.0;
+        for (int k = 0; k < K; ++k) {
+            long long *d = ca.lost_acc + 3 * k;
+            lost += fix_value(d, b_lost) / ca.scales[k];
+            d[0] = d[1] = d[2] = 0;
+        }
+        sc->lost_step = lost;
+        sc->lostenergy += lost;
+    }
+    const double a = ca.a, c = ca.c, dt = sc->dt;
+    const bool first = sc->t == 0.0;
+    const double one[1] = {1.0};
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+        if (first) {
+            double T = ca.temp[i];
+            double v[10] = {ca.fleck[i], ca.sa[i], a, c, T, T, T, T, dt, ca.ds};
+            int j;
+            ca.matenergydens[i] = sorter<0>(v, 10, one, 1, &j);
+        }
+        double inc = 0.0;
+        for (int k = 0; k < K; ++k)
+            inc += (ca.energydep[(size_t)k * nc + i] - ca.emitted[(size_t)k * nc + i]) / ca.scales[k];
+        double m = ca.matenergydens[i] + inc;
+        ca.matenergydens[i] = m;
+        if (ca.linearized) ca.temp[i] = pow(m, 0.25);
+        else ca.temp[i] = ca.temp[i] + inc / ca.bee[i];
+    }
+    double totdep = 0.0;
+    for (int k = 0; k < K; ++k) {
+        const double sk = ca.scales[k];
+        totdep += block_dd_sum(nc, [&](int i) { return (ca.energydep[(size_t)k * nc + i] * cell_vol(ca, i)) / sk; }, sh);
+    }
+    if (threadIdx.x == 0) sc->totalenergydep = totdep;
+}
+
+void launch_tally(const CellArgs &ca, Scalars *sc, cudaStream_t st) { k_tally<<<1, kPlanThreads, 0, st>>>(ca, sc); }
+
+__global__ void __launch_bounds__(kPlanThreads) k_energycheck(CellArgs ca, Scalars *sc, DevStats *stats,
+                                                              long long stats_cap) {
+    __shared__ DD sh[kPlanThreads];
+    double radenergy = block_dd_sum(ca.nc, [&](int i) { return ca.radenergydens[i] * cell_vol(ca, i); }, sh);
+    if (threadIdx.x == 0) {
+        double err = (sc->totalenergy - sc->totalenergydep - (radenergy - sc->radenergyold) - sc->lostenergy) /
+                     sc->totalenergy;
+        if (stats && stats_cap > 0) {
+            DevStats &d = stats[sc->step % (unsigned long long)stats_cap];
+            d.t = sc->t; d.dt = sc->dt;
+            d.total_energy = sc->totalenergy;
+            d.energy_dep = sc->totalenergydep;
+            d.rad_energy = radenergy;
+            d.rad_energy_old = sc->radenergyold;
+            d.lost_energy = sc->lostenergy;
+            d.energy_error = err;
+            d.n_census_in = sc->n_census_in;
+            d.n_sourced = sc->n_sourced;
+            d.n_census_out = sc->n_census;
+            d.segments = (long long)sc->segments;
+            d.surrogate_calls = (long long)sc->surrogate_calls;
+            d.error_flags = sc->flags;
+            d.step_index = sc->step;
+        }
+        sc->energy_err = err;
+        sc->radenergy = radenergy;
+        sc->radenergyold = radenergy;
+        sc->lostenergy = 0.0;
+    }
+}
+
+void launch_energycheck(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap, cudaStream_t st) {
+    k_energycheck<<<1, kPlanThreads, 0, st>>>(ca, sc, stats, stats_cap);
+}
+
+// timestep (src/MixedPrecisionIMC.jl:181-222), FP64 on the device so a run
+// can replay without host round trips.
+__global__ void k_timestep(CellArgs ca, Scalars *sc) {
+    double t = sc->t, dt = sc->dt;
+    const double t_end = ca.t_end;
+    if (t == t_end) {
+        t = t_end + dt;
+    } else if (ca.timestepping == 0) {
+        if (t + dt > t_end) { dt = t_end - t; t = t_end; }
+        else t = t + dt;
+    } else {
+        if (dt < ca.dtmax) {
+            dt = dt * ca.kfac;
+            if (dt > ca.dtmax) dt = ca.dtmax;
+        }
+        if (t + dt > t_end) { dt = t_end - t; t = t_end; }
+        else t = t + dt;
+    }
+    sc->t = t;
+    sc->dt = dt;
+    sc->finished = t > t_end ? 1 : 0;
+    sc->step += 1u;
+}
+
+void launch_timestep(const CellArgs &ca, Scalars *sc, cudaStream_t st) { k_timestep<<<1, 1, 0, st>>>(ca, sc); }
+
+// Transport of a list that was set directly (no sourcing this step): take the
+// fixed-point exponents from the census maximum.
+__global__ void k_prepare_transport(CellArgs ca, Scalars *sc) {
+    double emax = __longlong_as_double((long long)sc->emax_census_bits);
+    sc->emax = emax;
+    sc->emax_census_bits = 0ull;
+    sc->segments = 0ull;
+    sc->surrogate_calls = 0ull;
+    sc->n_census_in = sc->n_census;
+    sc->n_sourced = 0;
+    sc->n_particles = sc->n_census;
+    sc->b_dep = fix_exponent(emax / ca.vol_min);
+    sc->b_lost = fix_exponent(emax);
+    sc->b_rad = fix_exponent(emax);
+}
+
+void launch_prepare_transport(const CellArgs &ca, Scalars *sc, cudaStream_t st) {
+    k_prepare_transport<<<1, 1, 0, st>>>(ca, sc);
+}
+
+}  // namespace imc

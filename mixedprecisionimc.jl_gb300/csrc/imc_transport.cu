@@ -1,0 +1,433 @@
+// imc_transport.cu -- history-based particle transport, one thread per history.
+//
+//   k_transport1d <- Transport.MC   (src/imc_transport.jl:13-210)
+//   k_transport2d <- Transport.MC2D (src/imc_transport.jl:483-732)
+//
+// A persistent grid walks the particle list with a grid stride, so every
+// warp loads 32 consecutive particles (coalesced structure-of-arrays loads)
+// and keeps the whole history in registers: each particle's state is read
+// once and written once per step.  The per-cell transport table (sigma_a*f,
+// effective scatter, face widths) is built in shared memory by every block.
+//
+// Tallies: a history accumulates its deposits for the cell it is in as a
+// Neumaier-compensated pair in the arithmetic type, and flushes the pair when
+// it leaves the cell or ends, as exact fixed-point limbs (imc_device.cuh) with
+// 64-bit integer atomics.  Census energy and escaped energy are tallied the
+// same way.  All tallies are therefore independent of scheduling.
+//
+// The event logic restates the reference line by line: distances to the face,
+// to collision (randexp over the effective scatter opacity) and to census; the
+// minimum wins; events are tested by float equality in the reference's
+// if/if/if order, so ties run every matching branch, as they do there.
+#include <cstdint>
+#include "imc_device.cuh"
+#include "imc_internal.h"
+#include "imc_state.cuh"
+
+namespace imc {
+
+__device__ __forceinline__ float m_exp(float x) { return expf(x); }
+__device__ __forceinline__ double m_exp(double x) { return exp(x); }
+__device__ __forceinline__ float m_expm1(float x) { return expm1f(x); }
+__device__ __forceinline__ double m_expm1(double x) { return expm1(x); }
+__device__ __forceinline__ float m_abs(float x) { return fabsf(x); }
+__device__ __forceinline__ double m_abs(double x) { return fabs(x); }
+__device__ __forceinline__ void m_sincos(float a, float *s, float *c) { sincosf(a, s, c); }
+__device__ __forceinline__ void m_sincos(double a, double *s, double *c) { sincos(a, s, c); }
+
+// Neumaier compensated add; all deposit terms are non-negative.
+template <class T> __device__ __forceinline__ void nadd(T &s, T &c, T x) {
+    T t = s + x;
+    if (s >= x) c += (s - t) + x;
+    else c += (x - t) + s;
+    s = t;
+}
+
+__device__ __forceinline__ void add_limbs(long long *a, const Limbs &L) {
+    if (L.l0) atomicAdd((unsigned long long *)(a + 0), (unsigned long long)L.l0);
+    if (L.l1) atomicAdd((unsigned long long *)(a + 1), (unsigned long long)L.l1);
+    if (L.l2) atomicAdd((unsigned long long *)(a + 2), (unsigned long long)L.l2);
+}
+
+// flush a compensated pair (s, c) into accumulator slot
+template <class T>
+__device__ __forceinline__ void flush_pair(long long *acc, int slot, T s, T c, int b, unsigned &flags) {
+    if (s == (T)0 && c == (T)0) return;
+    Limbs A, B;
+    bool ok = fix_split(s, b, A) && fix_split(c, b, B);
+    if (!ok) {
+        flags |= (s != s || c != c) ? 1u /*NAN*/ : (1u << 5) /*FIXPOINT_RANGE*/;
+        return;
+    }
+    A.l0 += B.l0; A.l1 += B.l1; A.l2 += B.l2;
+    add_limbs(acc + 3 * (size_t)slot, A);
+}
+
+template <class T>
+__device__ __forceinline__ void flush_one(long long *acc, int slot, T v, int b, unsigned &flags) {
+    if (v == (T)0) return;
+    Limbs A;
+    if (!fix_split(v, b, A)) {
+        flags |= (v != v) ? 1u : (1u << 5);
+        return;
+    }
+    add_limbs(acc + 3 * (size_t)slot, A);
+}
+
+template <class T> struct Tab1 { T saf, seff, dxs, dxT; };
+template <class T> struct Tab2 { T saf, seff; };
+template <class T> struct Face { T ws, wT; };  // width * distancescale, width
+
+// end-of-kernel reduction of per-thread counters: one atomic per warp
+template <class T>
+__device__ __forceinline__ void finish_counters(Scalars *sc, unsigned long long segs, unsigned flags, T emax) {
+    const unsigned full = 0xFFFFFFFFu;
+    double em = (double)emax;
+    for (int off = 16; off > 0; off >>= 1) {
+        segs += __shfl_down_sync(full, segs, off);
+        flags |= __shfl_down_sync(full, flags, off);
+        double o = __shfl_down_sync(full, em, off);
+        em = o > em ? o : em;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (segs) atomicAdd(&sc->segments, segs);
+        if (flags) atomicOr(&sc->flags, flags);
+        if (em > 0.0) atomicMax(&sc->emax_census_bits, (unsigned long long)d2u(em));
+    }
+}
+
+template <class St>
+__global__ void __launch_bounds__(256) k_transport1d(CellArgs ca, Scalars *sc, PBufRaw raw) {
+    typedef typename St::T T;
+    PBuf<St> pb(raw);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Tab1<T> *tab = reinterpret_cast<Tab1<T> *>(smem_raw);
+    const int N = ca.nx;
+    const T ds = (T)ca.ds, c = (T)ca.c;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        T sa = (T)ca.sa[i], f = (T)ca.fleck[i], ss = (T)ca.ss[i];
+        Tab1<T> e;
+        e.saf = sa * f;
+        e.seff = sa * ((T)1 - f) + ss;
+        e.dxT = (T)ca.dx[i];
+        e.dxs = e.dxT * ds;
+        tab[i] = e;
+    }
+    __syncthreads();
+    const T endsteptime = (T)sc->dt;
+    const long long n = sc->n_particles;
+    const int b_dep = sc->b_dep, b_rad = sc->b_rad, b_lost = sc->b_lost;
+    const unsigned step = sc->step;
+    const unsigned long long seed = ca.seed;
+    const long long cap = ca.seg_cap;
+    const int nc = ca.nc;
+    const bool reflect_r = ca.bc[1] == 1, reflect_l = ca.bc[0] == 1;
+    unsigned long long segs = 0;
+    unsigned flags = 0;
+    T emax = (T)0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (!pb.alive[i]) continue;
+        const int cs = pb.cs[i];
+        int cell = cs & 0xFFFFFF;
+        const int k = cs >> 24;
+        T t, x, mu, E, E0;
+        E0 = (T)pb.E0[i];
+        if (St::half) {
+            t = ld_f(pb.t + i) * (float)endsteptime;
+            x = ld_f(pb.x + i) * (float)tab[cell].dxs;
+            mu = ld_f(pb.ux + i);
+            E = ld_f(pb.E + i) * (float)E0;
+        } else {
+            t = (T)pb.t[i]; x = (T)pb.x[i]; mu = (T)pb.ux[i]; E = (T)pb.E[i];
+        }
+        Stream rs;
+        rs.init(seed, step, (uint32_t)i, kStageTransport);
+        const T minenergy = (T)(0.01 * (double)E0);
+        T acc_s = (T)0, acc_c = (T)0;
+        int acc_cell = cell;
+        bool alive = true;
+        long long seg = 0;
+        while (true) {
+            if (++seg > cap) { flags |= (1u << 2); alive = false; break; }
+            const Tab1<T> ce = tab[cell];
+            T dist_b = mu > (T)0 ? (ce.dxs - x) / mu : m_abs(x / mu);
+            T dist_col = Rand<T>::exp1(rs) / ce.seff;
+            T dist_cen = c * (endsteptime - t) * ds;
+            T dist = jmin(jmin(dist_b, dist_col), dist_cen);
+            if (dist != dist) { flags |= 1u; alive = false; break; }
+            T newenergy = E * m_exp(-ce.saf * dist);
+            if (cell != acc_cell) {
+                flush_pair(ca.dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+                acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
+            }
+            if (newenergy <= minenergy) {
+                nadd(acc_s, acc_c, E / ce.dxT);
+                alive = false;
+                break;
+            }
+            nadd(acc_s, acc_c, -(E / ce.dxT) * m_expm1(-ce.saf * dist));
+            x += mu * dist;
+            t += (dist / ds) / c;
+            E = newenergy;
+            if (dist == dist_b) {
+                if (mu > (T)0) {
+                    if (cell == N - 1) {
+                        if (reflect_r) {
+                            mu = -mu;
+                        } else {
+                            flush_one(ca.lost_acc, k, E, b_lost, flags);
+                            alive = false;
+                            break;
+                        }
+                    }
+                    cell += 1;
+                    x = (T)0;
+                }
+                if (mu < (T)0) {
+                    if (cell == 0) {
+                        if (reflect_l) {
+                            mu = -mu;
+                        } else {
+                            flush_one(ca.lost_acc, k, E, b_lost, flags);
+                            alive = false;
+                            break;
+                        }
+                    } else {
+                        cell -= 1;
+                        x = tab[cell].dxs;
+                    }
+                }
+            }
+            if (dist == dist_col) {
+                // mu = 1 - 2*rand, redrawn while zero (src/imc_transport.jl:178-181);
+                // a zero needs rand == 0.5 exactly, so 64 redraws never run out
+                mu = (T)0;
+                for (int r = 0; r < 64 && mu == (T)0; ++r) mu = (T)1 - (T)2 * Rand<T>::u(rs);
+                if (mu == (T)0) mu = (T)1;
+            }
+            if (dist == dist_cen) {
+                // census: t = 0, write the state back (src/imc_transport.jl:185-193)
+                T Est = E;
+                if (St::half) {
+                    st_v(pb.t + i, 0.0f);
+                    st_v(pb.x + i, (float)x / (float)tab[cell].dxs);
+                    st_v(pb.ux + i, (float)mu);
+                    __half ef = __float2half_rn((float)E / (float)E0);
+                    pb.E[i] = ef;
+                    Est = __half2float(ef) * (float)E0;
+                } else {
+                    pb.t[i] = (typename St::S)0;
+                    pb.x[i] = (typename St::S)x;
+                    pb.ux[i] = (typename St::S)mu;
+                    pb.E[i] = (typename St::S)E;
+                }
+                if (cell != (cs & 0xFFFFFF)) pb.cs[i] = cell | (k << 24);
+                flush_one(ca.rad_acc, k * nc + cell, Est, b_rad, flags);
+                emax = Est > emax ? Est : emax;
+                break;
+            }
+        }
+        flush_pair(ca.dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+        if (!alive) pb.alive[i] = 0;
+        segs += (unsigned long long)seg;
+    }
+    finish_counters<T>(sc, segs, flags, emax);
+}
+
+template <class St>
+__global__ void __launch_bounds__(256) k_transport2d(CellArgs ca, Scalars *sc, PBufRaw raw) {
+    typedef typename St::T T;
+    PBuf<St> pb(raw);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int NX = ca.nx, NY = ca.ny, nc = ca.nc;
+    Tab2<T> *tab = reinterpret_cast<Tab2<T> *>(smem_raw);
+    Face<T> *fx = reinterpret_cast<Face<T> *>(tab + nc);
+    Face<T> *fy = fx + NX;
+    const T ds = (T)ca.ds, c = (T)ca.c;
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+        T sa = (T)ca.sa[i], f = (T)ca.fleck[i], ss = (T)ca.ss[i];
+        Tab2<T> e;
+        e.saf = sa * f;
+        e.seff = sa * ((T)1 - f) + ss;
+        tab[i] = e;
+    }
+    for (int i = threadIdx.x; i < NX; i += blockDim.x) { fx[i].wT = (T)ca.dx[i]; fx[i].ws = fx[i].wT * ds; }
+    for (int i = threadIdx.x; i < NY; i += blockDim.x) { fy[i].wT = (T)ca.dy[i]; fy[i].ws = fy[i].wT * ds; }
+    __syncthreads();
+    const T dtT = (T)sc->dt;
+    const long long n = sc->n_particles;
+    const int b_dep = sc->b_dep, b_rad = sc->b_rad, b_lost = sc->b_lost;
+    const unsigned step = sc->step;
+    const unsigned long long seed = ca.seed;
+    const long long cap = ca.seg_cap;
+    const bool refl_l = ca.bc[0] == 1, refl_r = ca.bc[1] == 1, refl_t = ca.bc[2] == 1, refl_b = ca.bc[3] == 1;
+    unsigned long long segs = 0;
+    unsigned flags = 0;
+    T emax = (T)0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (!pb.alive[i]) continue;
+        const int cs = pb.cs[i];
+        const int cell0 = cs & 0xFFFFFF;
+        const int k = cs >> 24;
+        int xi = cell0 % NX, yi = cell0 / NX;
+        T t, xp, yp, vx, vy, E, E0;
+        E0 = (T)pb.E0[i];
+        if (St::half) {
+            t = ld_f(pb.t + i) * (float)dtT;
+            xp = ld_f(pb.x + i) * (float)fx[xi].ws;
+            yp = ld_f(pb.y + i) * (float)fy[yi].ws;
+            vx = ld_f(pb.ux + i);
+            vy = ld_f(pb.uy + i);
+            E = ld_f(pb.E + i) * (float)E0;
+        } else {
+            t = (T)pb.t[i]; xp = (T)pb.x[i]; yp = (T)pb.y[i];
+            vx = (T)pb.ux[i]; vy = (T)pb.uy[i]; E = (T)pb.E[i];
+        }
+        Stream rs;
+        rs.init(seed, step, (uint32_t)i, kStageTransport);
+        const T minenergy = (T)(0.01 * (double)E0);
+        T acc_s = (T)0, acc_c = (T)0;
+        int acc_cell = cell0;
+        bool alive = true;
+        long long seg = 0;
+        while (true) {
+            if (++seg > cap) { flags |= (1u << 2); alive = false; break; }
+            T dist_bx = vx > (T)0 ? m_abs((fx[xi].ws - xp) / vx) : m_abs(xp / vx);
+            T dist_by = vy > (T)0 ? m_abs((fy[yi].ws - yp) / vy) : m_abs(yp / vy);
+            T dist_b;
+            if (dist_bx != dist_bx) dist_b = dist_by;
+            else if (dist_by != dist_by) dist_b = dist_bx;
+            else dist_b = jmin(dist_bx, dist_by);
+            const int cell = xi + yi * NX;
+            const Tab2<T> ce = tab[cell];
+            T dist_col = Rand<T>::exp1(rs) / ce.seff;
+            T dist_cen = c * (dtT - t) * ds;
+            T dist = jmin(jmin(dist_b, dist_col), dist_cen);
+            if (dist != dist) { flags |= 1u; alive = false; break; }
+            T newenergy = E * m_exp(-ce.saf * dist);
+            if (cell != acc_cell) {
+                flush_pair(ca.dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+                acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
+            }
+            const T Edens = (E / fx[xi].wT) / fy[yi].wT;
+            if (newenergy <= minenergy) {
+                nadd(acc_s, acc_c, Edens);
+                alive = false;
+                break;
+            }
+            nadd(acc_s, acc_c, -Edens * m_expm1(-ce.saf * dist));
+            xp += dist * vx;
+            yp += dist * vy;
+            t += (dist / ds) / c;
+            E = newenergy;
+            if (dist == dist_bx || dist == dist_by) {
+                if (dist_bx < dist_by) {
+                    if (vx > (T)0) {
+                        if (xi == NX - 1) {
+                            if (refl_r) { vx = -vx; continue; }
+                            flush_one(ca.lost_acc, k, E, b_lost, flags);
+                            alive = false;
+                            break;
+                        }
+                        xi += 1; xp = (T)0;
+                    } else {
+                        if (xi == 0) {
+                            if (refl_l) { vx = -vx; continue; }
+                            flush_one(ca.lost_acc, k, E, b_lost, flags);
+                            alive = false;
+                            break;
+                        }
+                        xi -= 1; xp = fx[xi].ws;
+                    }
+                } else {
+                    if (vy > (T)0) {
+                        if (yi == NY - 1) {
+                            if (refl_t) { vy = -vy; continue; }
+                            flush_one(ca.lost_acc, k, E, b_lost, flags);
+                            alive = false;
+                            break;
+                        }
+                        yi += 1; yp = (T)0;
+                    } else {
+                        if (yi == 0) {
+                            if (refl_b) { vy = -vy; continue; }
+                            flush_one(ca.lost_acc, k, E, b_lost, flags);
+                            alive = false;
+                            break;
+                        }
+                        yi -= 1; yp = fy[yi].ws;
+                    }
+                }
+                continue;
+            }
+            if (dist == dist_col) {
+                // isotropic re-emission: angle 2*pi*rand in Float64, rounded to T
+                T ang = (T)(6.283185307179586 * (double)Rand<T>::u(rs));
+                m_sincos(ang, &vy, &vx);
+            }
+            if (dist == dist_cen) {
+                const int cellf = xi + yi * NX;
+                T Est = E;
+                if (St::half) {
+                    st_v(pb.t + i, 0.0f);
+                    st_v(pb.x + i, (float)xp / (float)fx[xi].ws);
+                    st_v(pb.y + i, (float)yp / (float)fy[yi].ws);
+                    st_v(pb.ux + i, (float)vx);
+                    st_v(pb.uy + i, (float)vy);
+                    __half ef = __float2half_rn((float)E / (float)E0);
+                    pb.E[i] = ef;
+                    Est = __half2float(ef) * (float)E0;
+                } else {
+                    pb.t[i] = (typename St::S)0;
+                    pb.x[i] = (typename St::S)xp;
+                    pb.y[i] = (typename St::S)yp;
+                    pb.ux[i] = (typename St::S)vx;
+                    pb.uy[i] = (typename St::S)vy;
+                    pb.E[i] = (typename St::S)E;
+                }
+                if (cellf != cell0) pb.cs[i] = cellf | (k << 24);
+                flush_one(ca.rad_acc, k * nc + cellf, Est, b_rad, flags);
+                emax = Est > emax ? Est : emax;
+                break;
+            }
+        }
+        flush_pair(ca.dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+        if (!alive) pb.alive[i] = 0;
+        segs += (unsigned long long)seg;
+    }
+    finish_counters<T>(sc, segs, flags, emax);
+}
+
+int transport_smem_bytes(const CellArgs &ca, int prec) {
+    size_t tsz = prec == 0 ? sizeof(double) : sizeof(float);
+    if (ca.geometry == 1) return (int)(4 * tsz * (size_t)ca.nx);
+    return (int)(2 * tsz * ((size_t)ca.nc + ca.nx + ca.ny));
+}
+
+const void *transport_kernel_ptr(const CellArgs &ca, int prec) {
+    if (ca.geometry == 1) {
+        if (prec == 0) return (const void *)k_transport1d<StF64>;
+        if (prec == 1) return (const void *)k_transport1d<StF32>;
+        return (const void *)k_transport1d<StF16>;
+    }
+    if (prec == 0) return (const void *)k_transport2d<StF64>;
+    if (prec == 1) return (const void *)k_transport2d<StF32>;
+    return (const void *)k_transport2d<StF16>;
+}
+
+void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, int block, cudaStream_t st) {
+    int smem = transport_smem_bytes(ca, prec);
+    if (ca.geometry == 1) {
+        if (prec == 0) k_transport1d<StF64><<<grid, block, smem, st>>>(ca, sc, buf);
+        else if (prec == 1) k_transport1d<StF32><<<grid, block, smem, st>>>(ca, sc, buf);
+        else k_transport1d<StF16><<<grid, block, smem, st>>>(ca, sc, buf);
+    } else {
+        if (prec == 0) k_transport2d<StF64><<<grid, block, smem, st>>>(ca, sc, buf);
+        else if (prec == 1) k_transport2d<StF32><<<grid, block, smem, st>>>(ca, sc, buf);
+        else k_transport2d<StF16><<<grid, block, smem, st>>>(ca, sc, buf);
+    }
+}
+
+}  // namespace imc

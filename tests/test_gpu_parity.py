@@ -1,0 +1,147 @@
+"""GPU parity: each CUDA stage against the CPU oracle on the same deck, the
+same Philox streams and the same input state.
+
+Tolerances: FP64 state -- the kernels and the oracle share every formula,
+and differ only where CUDA's exp/expm1/log/pow round differently from
+glibc's (1-2 ulp), so per-particle states agree to 1e-12 relative and
+tallies to 1e-10.  FP32 state -- same, at single-precision ulps: 1e-4 relative
+per particle, with a small fraction of histories allowed to take a different
+branch after an ulp-level tie.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_deck
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(name, gpu_lib, **ov):
+    import mpimc
+    import oracle
+    inputs, mesh = load_deck(name, **ov)
+    return mpimc.Engine(inputs, mesh), oracle.Oracle(inputs, mesh)
+
+
+def _cmp_particles(g, o, rtol, frac_ok=1.0, keys=("t", "x", "mu", "E", "E0")):
+    pg, po = g.particles(), o.particles()
+    assert len(pg["E"]) == len(po["E"])
+    n = len(pg["E"])
+    if n == 0:
+        return
+    same_cell = pg["cell"] == po["cell"]
+    alive_g, alive_o = pg["E0"] >= 0, po["E0"] >= 0
+    ok = same_cell & (alive_g == alive_o) & (pg["scale"] == po["scale"])
+    for k in keys:
+        a, b = pg[k], po[k]
+        close = np.abs(a - b) <= rtol * np.maximum(np.abs(b), 1e-300) + 1e-300
+        ok &= close | ~alive_o
+    frac = ok.mean()
+    assert frac >= frac_ok, "only %.6f of %d particles agree" % (frac, n)
+
+
+@pytest.mark.parametrize("deck", ["tiny_1d", "tiny_2d", "c1_slab"])
+def test_update_parity(deck, gpu_lib):
+    g, o = _pair(deck, gpu_lib)
+    g.update()
+    o.update()
+    for f in ("fleck", "beta", "sigma_a", "sigma_s", "bee"):
+        np.testing.assert_allclose(g.field(f), o.field(f), rtol=1e-14, atol=0, err_msg=f)
+
+
+@pytest.mark.parametrize("deck", ["tiny_1d", "tiny_2d", "c1_slab"])
+def test_sourcing_parity(deck, gpu_lib):
+    g, o = _pair(deck, gpu_lib)
+    for e in (g, o):
+        e.update()
+        e.sourcing()
+    assert g.num_particles() == o.num_particles() > 0
+    np.testing.assert_allclose(g.field("emittedenergy"), o.field("emittedenergy"), rtol=1e-14)
+    keys = ("t", "x", "mu", "E", "E0") if g.geometry == 1 else ("t", "x", "y", "ux", "uy", "E", "E0")
+    _cmp_particles(g, o, rtol=1e-14, keys=keys)
+
+
+@pytest.mark.parametrize("deck", ["tiny_1d", "tiny_2d", "c1_slab"])
+def test_transport_parity_fp64(deck, gpu_lib):
+    g, o = _pair(deck, gpu_lib)
+    for e in (g, o):
+        e.update()
+        e.sourcing()
+        e.transport()
+    keys = ("t", "x", "mu", "E") if g.geometry == 1 else ("t", "x", "y", "E")
+    _cmp_particles(g, o, rtol=1e-10, frac_ok=0.999, keys=keys)
+    dg, do = g.field("energydep"), o.field("energydep")
+    np.testing.assert_allclose(dg, do, rtol=1e-8, atol=1e-12 * np.abs(do).max())
+
+
+@pytest.mark.parametrize("deck", ["tiny_1d", "tiny_2d", "c1_slab", "infinite_medium"])
+def test_step_parity_fp64(deck, gpu_lib):
+    """Three full steps: temperatures, radiation and material energy track the
+    oracle because both consume the same variates."""
+    g, o = _pair(deck, gpu_lib)
+    for _ in range(3):
+        sg, _ = g.step()
+        so, _ = o.step()
+        assert sg["n_sourced"] == so["n_sourced"]
+        assert abs(sg["n_census_out"] - so["n_census_out"]) <= max(2, 1e-4 * so["n_census_out"])
+        np.testing.assert_allclose(sg["total_energy"], so["total_energy"], rtol=1e-13)
+        np.testing.assert_allclose(sg["energy_error"], so["energy_error"], atol=1e-9)
+    for f in ("temp", "radenergydens", "matenergydens"):
+        a, b = g.field(f), o.field(f)
+        np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-9 * np.abs(b).max(), err_msg=f)
+
+
+def test_transport_parity_fp32(gpu_lib):
+    g, o = _pair("tiny_1d", gpu_lib, PRECISION=np.float32)
+    for e in (g, o):
+        e.update()
+        e.sourcing()
+    _cmp_particles(g, o, rtol=0, keys=("t", "x", "mu", "E", "E0"))
+    for e in (g, o):
+        e.transport()
+    _cmp_particles(g, o, rtol=1e-4, frac_ok=0.99, keys=("x", "mu", "E"))
+    dg, do = g.field("energydep"), o.field("energydep")
+    np.testing.assert_allclose(dg, do, rtol=1e-3, atol=1e-6 * np.abs(do).max())
+
+
+def test_energy_conservation_fp64(gpu_lib):
+    """src/imc_energycheck.jl:34 balance: <= 1e-10 relative in FP64 (1D, no
+    2D source quirk)."""
+    import mpimc
+    inputs, mesh = load_deck("c1_slab")
+    g = mpimc.Engine(inputs, mesh)
+    steps, _ = g.run(max_steps=40)
+    assert len(steps) == 40
+    for s in steps:
+        assert abs(s["energy_error"]) <= 1e-10, s
+
+
+def test_run_matches_step(gpu_lib):
+    """The graph-replayed run and stage-by-stage steps give identical fields."""
+    import mpimc
+    inputs, mesh = load_deck("tiny_1d")
+    a = mpimc.Engine(inputs, mesh)
+    b = mpimc.Engine(inputs, mesh)
+    sa, _ = a.run()
+    sb = []
+    done = False
+    while not done:
+        st, done = b.step()
+        sb.append(st)
+    assert len(sa) == len(sb)
+    for f in ("temp", "radenergydens", "matenergydens", "energydep"):
+        np.testing.assert_array_equal(a.field(f), b.field(f), err_msg=f)
+
+
+def test_bit_reproducible(gpu_lib):
+    """Fixed-point tallies: two runs give bit-identical fields."""
+    import mpimc
+    inputs, mesh = load_deck("c1_slab", PRECISION=np.float32)
+    out = []
+    for _ in range(2):
+        e = mpimc.Engine(inputs, mesh)
+        e.run(max_steps=20)
+        out.append([e.field(f) for f in ("temp", "radenergydens", "energydep")])
+        e.close()
+    for x, y in zip(*out):
+        np.testing.assert_array_equal(x, y)
