@@ -1,0 +1,318 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 IMC engine on the 1D linearized slab workload:
+2000 cells (dx = 0.005), dt = 0.005 to t = 3 (601 timesteps), NINPUT 2e6,
+NMAX 2e7, FP32 particle state with FP64 material update (deck
+tests/golden/decks/c2_slab_fine.txt).
+
+One bench step is one full simulation (t = 0 -> 3).  Printed on one JSON line:
+  value        particle segments per second over the timed steps (device
+               time, inputs resident in HBM; the particle state, ~0.6 GB, is
+               larger than L2, so no flush is needed between steps)
+  fom          1/(relerr^2 * s), relerr = RMS over cells of the relative error
+               of the final cell temperature against the FP64 ensemble mean
+               (tests/golden/c2_fp64_mean.npz), s = seconds per simulation
+  fp64         the same deck with FP64 particle state (the plain FP64 GPU
+               path), its segments/s, relerr and FOM
+  e2e          segments/s through the public API with host buffers: deck
+               upload, run and the read-back of the cell fields per step
+  roofline     the transport kernel: algorithmic bytes per launch over its
+               CUDA-event duration, against the measured HBM copy bandwidth
+  cpu_baseline the oracle (CPU restatement) on this host's cores, sampled
+  clocks       SM clock samples taken during the timed region
+
+``--impl reference`` times the CPU restatement of the reference path on all
+host cores on the same deck and prints the same JSON line with impl=reference.
+Under torchrun (N > 1) every rank runs an independent replica (seed + rank)
+on its own GPU; value is the sum of segments over the max time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "mixedprecisionimc.jl_gb300")
+DECK = os.path.join(REPO, "tests", "golden", "decks", "c2_slab_fine.txt")
+REF_MEAN = os.path.join(REPO, "tests", "golden", "c2_fp64_mean.npz")
+PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
+METRIC = "FOM 1/(relerr²·s) & segments/s: learned+FP32 vs plain FP64 GPU at same error"
+WORKLOAD = ("1D linearized slab, 2000 cells dx=0.005, dt=0.005 to t=3.0 (601 timesteps), NINPUT=2e6, NMAX=2e7, "
+            "sigma_a=1, c=a=1, source 1.0 on [0,0.5], FP32 particle state, FP64 material update")
+# algorithmic bytes of the 1D FP32 transport kernel: every transported
+# particle reads t, x, mu, E, E0, cell|scale (4 B each) and its alive byte;
+# every census particle writes t, x, mu, E back
+READ_B, WRITE_B = 25, 16
+
+for _p in (PKG, os.path.join(REPO, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM MHz and throttle reasons)."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([v.strip() for v in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = sorted(float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit())
+        mx = max(float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 5 + i and s[5 + i].strip() == "Active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def load_deck(seed_offset=0, **ov):
+    import mpimc
+    inputs = mpimc.Input.readInputs(DECK)
+    inputs["SEED"] = str(int(inputs["SEED"]) + seed_offset)
+    inputs.update(ov)
+    mesh = mpimc.Mesh.mesh_generation(inputs)
+    return inputs, mesh
+
+
+def relerr(temp, ref):
+    import numpy as np
+    if ref is None:
+        return None
+    r = ref["temp"]
+    return float(np.sqrt(np.mean(((temp - r) / r) ** 2)))
+
+
+def load_ref():
+    import numpy as np
+    if not os.path.exists(REF_MEAN):
+        return None
+    z = np.load(REF_MEAN)
+    return {k: z[k] for k in z.files}
+
+
+def run_once(inputs, mesh, overrides=None, timing=False):
+    """One full simulation on the GPU; returns device ms, segments, histories,
+    transport timing and the final temperature."""
+    import mpimc
+    eng = mpimc.Engine(inputs, mesh, overrides)
+    try:
+        eng.set_timing(timing)
+        steps, ms = eng.run()
+        tr_ms, tr_n = eng.transport_timing()
+        temp = eng.field("temp")
+        kps = eng.kernels_per_step()
+    finally:
+        eng.close()
+    segs = sum(s["segments"] for s in steps)
+    hist = sum(s["n_census_in"] + s["n_sourced"] for s in steps)
+    flags = 0
+    for s in steps:
+        flags |= s["error_flags"]
+    moved = sum((s["n_census_in"] + s["n_sourced"]) * READ_B + s["n_census_out"] * WRITE_B for s in steps)
+    return {"ms": ms, "segments": segs, "histories": hist, "steps": len(steps), "transport_ms": tr_ms,
+            "transport_launches": tr_n, "temp": temp, "flags": flags, "bytes": moved, "kernels": kps * len(steps),
+            "energy_error": max(abs(s["energy_error"]) for s in steps)}
+
+
+def e2e_once(seed_offset):
+    """Public-API run with host buffers: build the deck on the host, create the
+    engine (uploads it), run, read the cell fields back, destroy."""
+    import numpy as np
+    import mpimc
+    inputs, mesh = load_deck(seed_offset)
+    d, keep = mpimc.build_deck(inputs, mesh)
+    h2d = sum(v.nbytes for v in keep.values())
+    t0 = time.perf_counter()
+    eng = mpimc.Engine(inputs, mesh)
+    steps, _ = eng.run()
+    fields = [eng.field(f) for f in ("temp", "radenergydens", "matenergydens")]
+    eng.close()
+    wall = time.perf_counter() - t0
+    d2h = sum(f.nbytes for f in fields) + len(steps) * 96
+    return wall, sum(s["segments"] for s in steps), h2d, d2h
+
+
+def cpu_baseline(threads, steps=120):
+    """The oracle on this host: `threads` replicas of the deck at 1/100 of
+    the particle counts, first `steps` timesteps; segments per second."""
+    import oracle
+    import mpimc
+    inputs, mesh = load_deck(0, NINPUT="20000", NMAX="200000")
+    d, keep = mpimc.build_deck(inputs, mesh)
+    secs, segs, hist = oracle.bench(d, threads, steps)
+    return {"value": segs / secs, "unit": "segments/s", "cores": threads, "kind": "port",
+            "sample": "oracle FP32 on the same deck at NINPUT=2e4, NMAX=2e5, first %d of 601 timesteps, "
+                      "%d replicas (seeds 12345+i), %.1f s" % (steps, threads, secs),
+            "histories_per_s": hist / secs}
+
+
+def bench_reference(args):
+    rank, world, _ = _env_rank()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline(threads, steps=60)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(threads, steps=60))
+    wall = time.perf_counter() - t0
+    v = sum(x["value"] for x in vals) / len(vals)
+    cb = dict(vals[-1])
+    cb["value"] = v
+    print(json.dumps({
+        "metric": METRIC, "value": v, "unit": "segments/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (in-repo deck, seeded Philox)",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "step": "one oracle sample (60 timesteps, 1/100 particles, all cores)",
+                   "reference": "reference is Julia, not installable here; CPU restatement (oracle port) timed"},
+        "cpu_baseline": cb,
+        "e2e": {"value": v, "unit": "segments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparator run")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    rank, world, local = _env_rank()
+    if world > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    if args.impl == "reference":
+        return bench_reference(args)
+    import numpy as np
+    import mpimc
+    from mpimc import _build
+    _build.build()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    ref = load_ref()
+    peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+    hbm = peaks.get("hbm_gbs")
+    inputs, mesh = load_deck(rank)
+    for _ in range(args.warmup):
+        run_once(inputs, mesh, timing=True)
+    if dist:
+        dist.barrier()
+    runs = []
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            runs.append(run_once(*load_deck(rank + 1000 * (i + 1)), timing=True))
+        wall = time.perf_counter() - t0
+    dev_ms = sum(r["ms"] for r in runs)
+    segs = sum(r["segments"] for r in runs)
+    hist = sum(r["histories"] for r in runs)
+    t_max = dev_ms
+    if dist:
+        import torch
+        tt = torch.tensor([dev_ms, segs, hist], dtype=torch.float64)
+        mx = tt.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tt, op=dist.ReduceOp.SUM)
+        t_max, segs, hist = float(mx[0]), float(tt[1]), float(tt[2])
+    if rank != 0:
+        return 0
+    value = segs / (t_max / 1000.0)
+    s_per_run = dev_ms / 1000.0 / args.steps
+    rel = [relerr(r["temp"], ref) for r in runs]
+    rel_m = None if rel[0] is None else float(np.sqrt(np.mean(np.square(rel))))
+    fom = None if rel_m is None else 1.0 / (rel_m ** 2 * s_per_run)
+    # roofline of the transport kernel
+    tr_ms = sum(r["transport_ms"] * r["transport_launches"] for r in runs)
+    tr_n = sum(r["transport_launches"] for r in runs)
+    bytes_per_launch = sum(r["bytes"] for r in runs) / max(tr_n, 1)
+    avg_ms = tr_ms / max(tr_n, 1)
+    achieved = bytes_per_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else None
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": (achieved / hbm) if (achieved and hbm) else None, "traffic": None,
+                "kernel": "k_transport1d<StF32>", "avg_launch_ms": avg_ms, "launches": tr_n,
+                "algorithmic_bytes_per_launch": bytes_per_launch,
+                "transport_share_of_step": tr_ms / dev_ms if dev_ms else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"}
+    out = {
+        "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (in-repo deck, seeded Philox streams)",
+        "config": {"workload": WORKLOAD, "step": "one full simulation t=0..3 (601 timesteps)",
+                   "l2": "inputs larger than L2 (particle state ~0.6 GB); no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "histories_per_s": hist / (t_max / 1000.0),
+        "relerr_T": rel_m, "fom": fom,
+        "energy_error_max": max(r["energy_error"] for r in runs),
+        "error_flags": int(np.bitwise_or.reduce([r["flags"] for r in runs])),
+        "gpu_launches": sum(r["kernels"] for r in runs),
+        "clocks": clk.summary(),
+        "roofline": roofline,
+        "wall_s_timed": wall,
+    }
+    if not args.no_fp64:
+        r64 = run_once(*load_deck(7), overrides={"precision": 0, "scale_select_precision": 0}, timing=False)
+        s64 = r64["ms"] / 1000.0
+        rel64 = relerr(r64["temp"], ref)
+        fom64 = None if rel64 is None else 1.0 / (rel64 ** 2 * s64)
+        out["fp64"] = {"value": r64["segments"] / s64, "unit": "segments/s", "ms_per_step": r64["ms"],
+                       "relerr_T": rel64, "fom": fom64, "energy_error_max": r64["energy_error"]}
+        if fom and fom64:
+            out["fom_ratio_fp32_over_fp64"] = fom / fom64
+    w, s, h2d, d2h = e2e_once(2000)
+    out["e2e"] = {"value": s / w, "unit": "segments/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                  "wall_s_per_step": w}
+    if not args.no_cpu:
+        try:
+            out["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1)
+        except Exception as e:  # the baseline is reported, never required
+            out["cpu_baseline"] = {"value": None, "error": str(e)}
+    print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -18,7 +18,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/imc.h"
+#include "imc.h"  // include/imc.h (on the -I path)
 #include "imc_internal.h"
 
 using namespace imc;
@@ -253,8 +253,9 @@ int enqueue_step(ImcHandle *h, int parity, bool with_events, int ev_slot) {
     launch_update(h->ca, h->d_sc, st);
     launch_source(h->ca, h->d_sc, h->prec, src, h->grid_emit, st);
     if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot], st));
-    launch_transport(h->ca, h->d_sc, h->prec, src, h->grid_transport, h->block_transport, st);
+    launch_transport(h->ca, h->d_sc, h->prec, src, h->grid_transport, st);
     if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot + 1], st));
+    launch_finalize(h->ca, h->d_sc, st);
     launch_compact(h->ca, h->d_sc, h->prec, src, dst, h->tile_cnt, h->tile_off, h->ntiles_cap, st);
     launch_tally(h->ca, h->d_sc, st);
     launch_energycheck(h->ca, h->d_sc, h->d_stats, h->stats_cap, st);
@@ -466,7 +467,9 @@ int imc_create(const ImcDeck *d, ImcHandle **out) {
         return bail(fail(h, IMC_ERR_CUDA, "upload scalars"));
     if ((rc = ensure_stats(h, 64))) return bail(rc);
     // launch shapes: persistent grids sized by occupancy on this GPU
-    int smem = transport_smem_bytes(ca, h->prec);
+    TransportShape shape = transport_shape(ca, h->prec);
+    const int smem = shape.smem;
+    h->block_transport = shape.block;
     const void *kp = transport_kernel_ptr(ca, h->prec);
     if (smem > 227 * 1024) return bail(fail(h, IMC_ERR_INVALID_ARG, "mesh too large for the shared-memory transport table"));
     if (smem > 48 * 1024)
@@ -524,7 +527,7 @@ int imc_transport(ImcHandle *h) {
     if (!h) return IMC_ERR_INVALID_ARG;
     if (h->stage != Stage::Sourced) launch_prepare_transport(h->ca, h->d_sc, h->stream);
     if (h->timing) CK(h, cudaEventRecord(h->ev[0], h->stream));
-    launch_transport(h->ca, h->d_sc, h->prec, h->buf[h->cur], h->grid_transport, h->block_transport, h->stream);
+    launch_transport(h->ca, h->d_sc, h->prec, h->buf[h->cur], h->grid_transport, h->stream);
     CKL(h);
     if (h->timing) {
         CK(h, cudaEventRecord(h->ev[1], h->stream));
@@ -534,6 +537,8 @@ int imc_transport(ImcHandle *h) {
         h->transport_ms += ms;
         h->transport_launches += 1;
     }
+    launch_finalize(h->ca, h->d_sc, h->stream);
+    CKL(h);
     Scalars sc;
     int rc = read_scalars(h, &sc);
     if (rc) return rc;
@@ -937,8 +942,8 @@ int imc_transport_timing(ImcHandle *h, double *avg_ms, int64_t *launches) {
 
 int imc_kernels_per_step(const ImcHandle *h, int *count) {
     if (!h || !count) return IMC_ERR_INVALID_ARG;
-    // update, source x3, transport, compact x4, tally, energycheck, timestep
-    *count = 12;
+    // update, source x3, transport, finalize, compact x4, tally, energycheck, timestep
+    *count = 13;
     return IMC_OK;
 }
 

@@ -76,8 +76,10 @@ struct Stream {
 template <class T> struct Rand;
 template <> struct Rand<float> {
     static IMC_HD float u(Stream &s) { return (float)(s.next() >> 8) * 0x1p-24f; }
+    // v = odd multiple of 2^-24 on (0,1): -log(v) is never 0 (so 0/0 cannot
+    // arise when the effective scatter opacity rounds to 0) and never inf
     static IMC_HD float exp1(Stream &s) {
-        float v = (float)((s.next() >> 8) + 1u) * 0x1p-24f;
+        float v = (float)((s.next() >> 8) | 1u) * 0x1p-24f;
         return -logf(v);
     }
 };
@@ -88,7 +90,7 @@ template <> struct Rand<double> {
     }
     static IMC_HD double exp1(Stream &s) {
         uint64_t hi = s.next(), lo = s.next();
-        double v = (double)((((hi << 32) | lo) >> 11) + 1u) * 0x1p-53;
+        double v = (double)((((hi << 32) | lo) >> 11) | 1u) * 0x1p-53;
         return -log(v);
     }
 };

@@ -81,14 +81,20 @@ struct DevStats {
 // launchers (imc_kernels.cu / imc_transport.cu); all asynchronous on `st`
 void launch_update(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, cudaStream_t st);
-void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, int block, cudaStream_t st);
+struct TransportShape {
+    bool smem_tally;  // block-private tallies in shared memory
+    int smem;         // dynamic shared memory bytes
+    int block;        // threads per block
+};
+TransportShape transport_shape(const CellArgs &ca, int prec);
+void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, cudaStream_t st);
 void launch_compact(const CellArgs &ca, Scalars *sc, int prec, PBufRaw src, PBufRaw dst, long long *tile_cnt,
                     long long *tile_off, long long ntiles_cap, cudaStream_t st);
+void launch_finalize(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 void launch_tally(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 void launch_energycheck(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap, cudaStream_t st);
 void launch_timestep(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 void launch_prepare_transport(const CellArgs &ca, Scalars *sc, cudaStream_t st);
-int transport_smem_bytes(const CellArgs &ca, int prec);
 const void *transport_kernel_ptr(const CellArgs &ca, int prec);
 
 constexpr int kCompactTile = 4096;     // particles per compaction tile

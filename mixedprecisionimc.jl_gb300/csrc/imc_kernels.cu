@@ -556,11 +556,13 @@ __device__ __forceinline__ double cell_vol(const CellArgs &ca, int i) {
     return ca.geometry == 1 ? ca.dx[i] : ca.dx[i % ca.nx] * ca.dy[i / ca.nx];
 }
 
-__global__ void __launch_bounds__(kPlanThreads) k_tally(CellArgs ca, Scalars *sc) {
-    __shared__ DD sh[kPlanThreads];
+// Converts this transport's fixed-point tallies to FP64 mesh fields and
+// clears the accumulators: energydep and the escaped energy as
+// Transport.MC leaves them (src/imc_transport.jl:198-205), and the census
+// radiation energy density of src/imc_tally.jl:81-113.
+__global__ void __launch_bounds__(kPlanThreads) k_finalize(CellArgs ca, Scalars *sc) {
     const int nc = ca.nc, K = ca.K;
     const int b_dep = sc->b_dep, b_rad = sc->b_rad, b_lost = sc->b_lost;
-    // finalise the fixed-point tallies of this step's transport
     for (int idx = threadIdx.x; idx < K * nc; idx += blockDim.x) {
         long long *d = ca.dep_acc + 3 * (size_t)idx;
         ca.energydep[idx] = fix_value(d, b_dep);
@@ -576,7 +578,6 @@ __global__ void __launch_bounds__(kPlanThreads) k_tally(CellArgs ca, Scalars *sc
         }
         ca.radenergydens[i] = r;
     }
-    __syncthreads();
     if (threadIdx.x == 0) {
         double lost = 0.0;
         for (int k = 0; k < K; ++k) {
@@ -587,6 +588,13 @@ __global__ void __launch_bounds__(kPlanThreads) k_tally(CellArgs ca, Scalars *sc
         sc->lost_step = lost;
         sc->lostenergy += lost;
     }
+}
+
+void launch_finalize(const CellArgs &ca, Scalars *sc, cudaStream_t st) { k_finalize<<<1, kPlanThreads, 0, st>>>(ca, sc); }
+
+__global__ void __launch_bounds__(kPlanThreads) k_tally(CellArgs ca, Scalars *sc) {
+    __shared__ DD sh[kPlanThreads];
+    const int nc = ca.nc, K = ca.K;
     const double a = ca.a, c = ca.c, dt = sc->dt;
     const bool first = sc->t == 0.0;
     const double one[1] = {1.0};

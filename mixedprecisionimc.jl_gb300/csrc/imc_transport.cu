@@ -43,14 +43,46 @@ template <class T> __device__ __forceinline__ void nadd(T &s, T &c, T x) {
     s = t;
 }
 
-__device__ __forceinline__ void add_limbs(long long *a, const Limbs &L) {
-    if (L.l0) atomicAdd((unsigned long long *)(a + 0), (unsigned long long)L.l0);
-    if (L.l1) atomicAdd((unsigned long long *)(a + 1), (unsigned long long)L.l1);
-    if (L.l2) atomicAdd((unsigned long long *)(a + 2), (unsigned long long)L.l2);
+// Limb adds into global memory (64-bit integer reductions in L2) or into the
+// block's private copy of the tally in shared memory.
+template <bool SMT> __device__ __forceinline__ void add_limbs(long long *a, const Limbs &L) {
+    if (SMT) {
+        // the pointer is known to address shared memory
+        unsigned long long *s = (unsigned long long *)a;
+        if (L.l0) atomicAdd_block(s + 0, (unsigned long long)L.l0);
+        if (L.l1) atomicAdd_block(s + 1, (unsigned long long)L.l1);
+        if (L.l2) atomicAdd_block(s + 2, (unsigned long long)L.l2);
+    } else {
+        if (L.l0) atomicAdd((unsigned long long *)(a + 0), (unsigned long long)L.l0);
+        if (L.l1) atomicAdd((unsigned long long *)(a + 1), (unsigned long long)L.l1);
+        if (L.l2) atomicAdd((unsigned long long *)(a + 2), (unsigned long long)L.l2);
+    }
+}
+
+// bytes of the per-cell transport table at the start of dynamic shared memory
+__host__ __device__ __forceinline__ int table_bytes(const CellArgs &ca, int tsz) {
+    int b = ca.geometry == 1 ? 4 * tsz * ca.nx : 2 * tsz * (ca.nc + ca.nx + ca.ny);
+    return (b + 15) & ~15;
+}
+
+__device__ __forceinline__ long long *tally_smem(unsigned char *smem, int table) {
+    return reinterpret_cast<long long *>(smem + table);
+}
+
+// Adds the block's shared tallies (deposition, then census energy, in the
+// same 3-limb layout as the global accumulators) to the global ones.
+__device__ __forceinline__ void flush_block_tallies(const CellArgs &ca, const long long *sm) {
+    __syncthreads();
+    const int n = 3 * ca.K * ca.nc;
+    for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) {
+        long long v = sm[i];
+        if (v) atomicAdd((unsigned long long *)((i < n ? ca.dep_acc : ca.rad_acc) + (i < n ? i : i - n)),
+                         (unsigned long long)v);
+    }
 }
 
 // flush a compensated pair (s, c) into accumulator slot
-template <class T>
+template <class T, bool SMT>
 __device__ __forceinline__ void flush_pair(long long *acc, int slot, T s, T c, int b, unsigned &flags) {
     if (s == (T)0 && c == (T)0) return;
     Limbs A, B;
@@ -60,10 +92,10 @@ __device__ __forceinline__ void flush_pair(long long *acc, int slot, T s, T c, i
         return;
     }
     A.l0 += B.l0; A.l1 += B.l1; A.l2 += B.l2;
-    add_limbs(acc + 3 * (size_t)slot, A);
+    add_limbs<SMT>(acc + 3 * (size_t)slot, A);
 }
 
-template <class T>
+template <class T, bool SMT>
 __device__ __forceinline__ void flush_one(long long *acc, int slot, T v, int b, unsigned &flags) {
     if (v == (T)0) return;
     Limbs A;
@@ -71,7 +103,7 @@ __device__ __forceinline__ void flush_one(long long *acc, int slot, T v, int b, 
         flags |= (v != v) ? 1u : (1u << 5);
         return;
     }
-    add_limbs(acc + 3 * (size_t)slot, A);
+    add_limbs<SMT>(acc + 3 * (size_t)slot, A);
 }
 
 template <class T> struct Tab1 { T saf, seff, dxs, dxT; };
@@ -96,14 +128,20 @@ __device__ __forceinline__ void finish_counters(Scalars *sc, unsigned long long 
     }
 }
 
-template <class St>
-__global__ void __launch_bounds__(256) k_transport1d(CellArgs ca, Scalars *sc, PBufRaw raw) {
+template <class St, int BLOCK, bool SMT>
+__global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc, PBufRaw raw) {
     typedef typename St::T T;
     PBuf<St> pb(raw);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Tab1<T> *tab = reinterpret_cast<Tab1<T> *>(smem_raw);
     const int N = ca.nx;
     const T ds = (T)ca.ds, c = (T)ca.c;
+    long long *dep_acc = ca.dep_acc, *rad_acc = ca.rad_acc;
+    if (SMT) {
+        dep_acc = tally_smem(smem_raw, table_bytes(ca, sizeof(T)));
+        rad_acc = dep_acc + 3 * (size_t)ca.K * ca.nc;
+        for (int i = threadIdx.x; i < 6 * ca.K * ca.nc; i += blockDim.x) dep_acc[i] = 0;
+    }
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
         T sa = (T)ca.sa[i], f = (T)ca.fleck[i], ss = (T)ca.ss[i];
         Tab1<T> e;
@@ -158,7 +196,7 @@ __global__ void __launch_bounds__(256) k_transport1d(CellArgs ca, Scalars *sc, P
             if (dist != dist) { flags |= 1u; alive = false; break; }
             T newenergy = E * m_exp(-ce.saf * dist);
             if (cell != acc_cell) {
-                flush_pair(ca.dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+                flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
                 acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
             }
             if (newenergy <= minenergy) {
@@ -176,7 +214,7 @@ __global__ void __launch_bounds__(256) k_transport1d(CellArgs ca, Scalars *sc, P
                         if (reflect_r) {
                             mu = -mu;
                         } else {
-                            flush_one(ca.lost_acc, k, E, b_lost, flags);
+                            flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
                             alive = false;
                             break;
                         }
@@ -189,7 +227,7 @@ __global__ void __launch_bounds__(256) k_transport1d(CellArgs ca, Scalars *sc, P
                         if (reflect_l) {
                             mu = -mu;
                         } else {
-                            flush_one(ca.lost_acc, k, E, b_lost, flags);
+                            flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
                             alive = false;
                             break;
                         }
@@ -223,20 +261,21 @@ __global__ void __launch_bounds__(256) k_transport1d(CellArgs ca, Scalars *sc, P
                     pb.E[i] = (typename St::S)E;
                 }
                 if (cell != (cs & 0xFFFFFF)) pb.cs[i] = cell | (k << 24);
-                flush_one(ca.rad_acc, k * nc + cell, Est, b_rad, flags);
+                flush_one<T, SMT>(rad_acc, k * nc + cell, Est, b_rad, flags);
                 emax = Est > emax ? Est : emax;
                 break;
             }
         }
-        flush_pair(ca.dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+        flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
         if (!alive) pb.alive[i] = 0;
         segs += (unsigned long long)seg;
     }
+    if (SMT) flush_block_tallies(ca, dep_acc);
     finish_counters<T>(sc, segs, flags, emax);
 }
 
-template <class St>
-__global__ void __launch_bounds__(256) k_transport2d(CellArgs ca, Scalars *sc, PBufRaw raw) {
+template <class St, int BLOCK, bool SMT>
+__global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc, PBufRaw raw) {
     typedef typename St::T T;
     PBuf<St> pb(raw);
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -245,6 +284,12 @@ __global__ void __launch_bounds__(256) k_transport2d(CellArgs ca, Scalars *sc, P
     Face<T> *fx = reinterpret_cast<Face<T> *>(tab + nc);
     Face<T> *fy = fx + NX;
     const T ds = (T)ca.ds, c = (T)ca.c;
+    long long *dep_acc = ca.dep_acc, *rad_acc = ca.rad_acc;
+    if (SMT) {
+        dep_acc = tally_smem(smem_raw, table_bytes(ca, sizeof(T)));
+        rad_acc = dep_acc + 3 * (size_t)ca.K * ca.nc;
+        for (int i = threadIdx.x; i < 6 * ca.K * ca.nc; i += blockDim.x) dep_acc[i] = 0;
+    }
     for (int i = threadIdx.x; i < nc; i += blockDim.x) {
         T sa = (T)ca.sa[i], f = (T)ca.fleck[i], ss = (T)ca.ss[i];
         Tab2<T> e;
@@ -308,7 +353,7 @@ __global__ void __launch_bounds__(256) k_transport2d(CellArgs ca, Scalars *sc, P
             if (dist != dist) { flags |= 1u; alive = false; break; }
             T newenergy = E * m_exp(-ce.saf * dist);
             if (cell != acc_cell) {
-                flush_pair(ca.dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+                flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
                 acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
             }
             const T Edens = (E / fx[xi].wT) / fy[yi].wT;
@@ -327,7 +372,7 @@ __global__ void __launch_bounds__(256) k_transport2d(CellArgs ca, Scalars *sc, P
                     if (vx > (T)0) {
                         if (xi == NX - 1) {
                             if (refl_r) { vx = -vx; continue; }
-                            flush_one(ca.lost_acc, k, E, b_lost, flags);
+                            flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
                             alive = false;
                             break;
                         }
@@ -335,7 +380,7 @@ __global__ void __launch_bounds__(256) k_transport2d(CellArgs ca, Scalars *sc, P
                     } else {
                         if (xi == 0) {
                             if (refl_l) { vx = -vx; continue; }
-                            flush_one(ca.lost_acc, k, E, b_lost, flags);
+                            flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
                             alive = false;
                             break;
                         }
@@ -345,7 +390,7 @@ __global__ void __launch_bounds__(256) k_transport2d(CellArgs ca, Scalars *sc, P
                     if (vy > (T)0) {
                         if (yi == NY - 1) {
                             if (refl_t) { vy = -vy; continue; }
-                            flush_one(ca.lost_acc, k, E, b_lost, flags);
+                            flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
                             alive = false;
                             break;
                         }
@@ -353,7 +398,7 @@ __global__ void __launch_bounds__(256) k_transport2d(CellArgs ca, Scalars *sc, P
                     } else {
                         if (yi == 0) {
                             if (refl_b) { vy = -vy; continue; }
-                            flush_one(ca.lost_acc, k, E, b_lost, flags);
+                            flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
                             alive = false;
                             break;
                         }
@@ -388,45 +433,68 @@ __global__ void __launch_bounds__(256) k_transport2d(CellArgs ca, Scalars *sc, P
                     pb.E[i] = (typename St::S)E;
                 }
                 if (cellf != cell0) pb.cs[i] = cellf | (k << 24);
-                flush_one(ca.rad_acc, k * nc + cellf, Est, b_rad, flags);
+                flush_one<T, SMT>(rad_acc, k * nc + cellf, Est, b_rad, flags);
                 emax = Est > emax ? Est : emax;
                 break;
             }
         }
-        flush_pair(ca.dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+        flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
         if (!alive) pb.alive[i] = 0;
         segs += (unsigned long long)seg;
     }
+    if (SMT) flush_block_tallies(ca, dep_acc);
     finish_counters<T>(sc, segs, flags, emax);
 }
 
-int transport_smem_bytes(const CellArgs &ca, int prec) {
-    size_t tsz = prec == 0 ? sizeof(double) : sizeof(float);
-    if (ca.geometry == 1) return (int)(4 * tsz * (size_t)ca.nx);
-    return (int)(2 * tsz * ((size_t)ca.nc + ca.nx + ca.ny));
+// Launch shape of the transport kernel.  When the table and the block's
+// private tallies fit in shared memory the kernel runs one large block per
+// SM with shared tallies (BLOCK 768 for FP32 / FP16 state, 512 for FP64);
+// otherwise 256-thread blocks with tallies in global memory.
+constexpr int kSmemBudget = 200 * 1024;
+
+TransportShape transport_shape(const CellArgs &ca, int prec) {
+    TransportShape sh;
+    const int tsz = prec == 0 ? 8 : 4;
+    const int table = table_bytes(ca, tsz);
+    const long long tallies = 2ll * 3 * 8 * (long long)ca.K * ca.nc;
+    sh.smem_tally = table + tallies <= kSmemBudget;
+    sh.smem = sh.smem_tally ? (int)(table + tallies) : table;
+    sh.block = sh.smem_tally ? (prec == 0 ? 512 : 768) : 256;
+    return sh;
+}
+
+template <class St, int B, bool SMT> static const void *kptr(int geometry) {
+    return geometry == 1 ? (const void *)k_transport1d<St, B, SMT> : (const void *)k_transport2d<St, B, SMT>;
 }
 
 const void *transport_kernel_ptr(const CellArgs &ca, int prec) {
-    if (ca.geometry == 1) {
-        if (prec == 0) return (const void *)k_transport1d<StF64>;
-        if (prec == 1) return (const void *)k_transport1d<StF32>;
-        return (const void *)k_transport1d<StF16>;
+    TransportShape sh = transport_shape(ca, prec);
+    if (sh.smem_tally) {
+        if (prec == 0) return kptr<StF64, 512, true>(ca.geometry);
+        if (prec == 1) return kptr<StF32, 768, true>(ca.geometry);
+        return kptr<StF16, 768, true>(ca.geometry);
     }
-    if (prec == 0) return (const void *)k_transport2d<StF64>;
-    if (prec == 1) return (const void *)k_transport2d<StF32>;
-    return (const void *)k_transport2d<StF16>;
+    if (prec == 0) return kptr<StF64, 256, false>(ca.geometry);
+    if (prec == 1) return kptr<StF32, 256, false>(ca.geometry);
+    return kptr<StF16, 256, false>(ca.geometry);
 }
 
-void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, int block, cudaStream_t st) {
-    int smem = transport_smem_bytes(ca, prec);
-    if (ca.geometry == 1) {
-        if (prec == 0) k_transport1d<StF64><<<grid, block, smem, st>>>(ca, sc, buf);
-        else if (prec == 1) k_transport1d<StF32><<<grid, block, smem, st>>>(ca, sc, buf);
-        else k_transport1d<StF16><<<grid, block, smem, st>>>(ca, sc, buf);
+template <class St, int B, bool SMT>
+static void launch_one(const CellArgs &ca, Scalars *sc, PBufRaw buf, int grid, int smem, cudaStream_t st) {
+    if (ca.geometry == 1) k_transport1d<St, B, SMT><<<grid, B, smem, st>>>(ca, sc, buf);
+    else k_transport2d<St, B, SMT><<<grid, B, smem, st>>>(ca, sc, buf);
+}
+
+void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, cudaStream_t st) {
+    TransportShape sh = transport_shape(ca, prec);
+    if (sh.smem_tally) {
+        if (prec == 0) launch_one<StF64, 512, true>(ca, sc, buf, grid, sh.smem, st);
+        else if (prec == 1) launch_one<StF32, 768, true>(ca, sc, buf, grid, sh.smem, st);
+        else launch_one<StF16, 768, true>(ca, sc, buf, grid, sh.smem, st);
     } else {
-        if (prec == 0) k_transport2d<StF64><<<grid, block, smem, st>>>(ca, sc, buf);
-        else if (prec == 1) k_transport2d<StF32><<<grid, block, smem, st>>>(ca, sc, buf);
-        else k_transport2d<StF16><<<grid, block, smem, st>>>(ca, sc, buf);
+        if (prec == 0) launch_one<StF64, 256, false>(ca, sc, buf, grid, sh.smem, st);
+        else if (prec == 1) launch_one<StF32, 256, false>(ca, sc, buf, grid, sh.smem, st);
+        else launch_one<StF16, 256, false>(ca, sc, buf, grid, sh.smem, st);
     }
 }
 

@@ -131,11 +131,12 @@ def make_simvars(inputs, mesh):
     """src/MixedPrecisionIMC.jl:88-125 (clock values kept in FP64)."""
     precision = inputs.get("PRECISION", np.float64)
     p = lambda k: float(precision(float(inputs[k])))
+    f64 = lambda k: float(inputs[k])  # the clock is FP64 for every PRECISION
     ts = str(inputs["TIMESTEPPING"]).upper()
     if ts == "CONSTANT":
-        dt, t_end, dt0, k, dtmax = p("DT"), p("ENDTIME"), 0.0, 0.0, 0.0
+        dt, t_end, dt0, k, dtmax = f64("DT"), f64("ENDTIME"), 0.0, 0.0, 0.0
     elif ts == "RAMP":
-        dt0, k, dtmax, t_end = p("DT0"), p("K"), p("DTMAX"), p("ENDTIME")
+        dt0, k, dtmax, t_end = f64("DT0"), f64("K"), f64("DTMAX"), f64("ENDTIME")
         dt = dt0
     else:
         raise ValueError("TIMESTEPPING must be CONSTANT or RAMP")

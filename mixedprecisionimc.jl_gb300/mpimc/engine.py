@@ -91,12 +91,15 @@ def build_deck(inputs, mesh, overrides=None):
     ts = str(inputs.get("TIMESTEPPING", "CONSTANT")).strip().upper()
     d.timestepping = _lib.IMC_TS_RAMP if ts == "RAMP" else _lib.IMC_TS_CONSTANT
     d.sort_census = 1 if _flag(inputs, "SORTCENSUS") else 0
+    # the clock is FP64 for every PRECISION (timestep control stays on the
+    # host in FP64), so DT / ENDTIME are not rounded to the deck precision
+    f64 = lambda k: float(inputs[k])
     if d.timestepping == _lib.IMC_TS_CONSTANT:
-        d.dt = p("DT")
+        d.dt = f64("DT")
     else:
-        d.dt0, d.k, d.dtmax = p("DT0"), p("K"), p("DTMAX")
+        d.dt0, d.k, d.dtmax = f64("DT0"), f64("K"), f64("DTMAX")
         d.dt = d.dt0
-    d.t_end = p("ENDTIME")
+    d.t_end = f64("ENDTIME")
     d.capacity = int(float(inputs.get("CAPACITY", 0)))
     d.segment_cap = int(float(inputs.get("SEGMENTCAP", 0)))
     for k, v in ov.items():

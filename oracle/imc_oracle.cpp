@@ -28,7 +28,7 @@
  *   - RNG: Julia's global Xoshiro stream is replaced by Philox-4x32-10 keyed
  *     (SEED, step, particle index, stage), identical to the GPU kernels, so a
  *     history here and on the GPU consume the same variates.  randexp() is
- *     -log(v), v uniform on (0,1] (the reference uses a ziggurat: same law).
+ *     -log(v), v uniform on (0,1) (the reference uses a ziggurat: same law).
  *   - Mesh-side arithmetic (update, sourcing energies, tally) is FP64 for every
  *     PRECISION; particle arithmetic follows PRECISION.  The energy-scale
  *     choice of sorter is still evaluated in the deck precision.

@@ -71,15 +71,16 @@ static inline double orc_rand_f64(OrcStream *s) {
     uint64_t lo = orc_next_u32(s);
     return (double)(((hi << 32) | lo) >> 11) * 0x1p-53;
 }
-/* exponential variate -log(v), v on (0,1] (the reference's randexp) */
+/* exponential variate -log(v) (the reference's randexp), v an odd multiple of
+ * 2^-24 (2^-53) on (0,1), so the variate is never 0 and never infinite */
 static inline float orc_randexp_f32(OrcStream *s) {
-    float v = (float)((orc_next_u32(s) >> 8) + 1u) * 0x1p-24f;
+    float v = (float)((orc_next_u32(s) >> 8) | 1u) * 0x1p-24f;
     return -logf(v);
 }
 static inline double orc_randexp_f64(OrcStream *s) {
     uint64_t hi = orc_next_u32(s);
     uint64_t lo = orc_next_u32(s);
-    double v = (double)((((hi << 32) | lo) >> 11) + 1u) * 0x1p-53;
+    double v = (double)((((hi << 32) | lo) >> 11) | 1u) * 0x1p-53;
     return -log(v);
 }
 

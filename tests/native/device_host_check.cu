@@ -1,0 +1,65 @@
+// Host-side check of imc_device.cuh (the __host__ __device__ paths): reads
+// commands on stdin, prints results on stdout.  Built and driven by
+// tests/test_device_header.py; needs no GPU.
+//   P c0 c1 c2 c3 k0 k1          -> philox4x32_10 words
+//   S seed step pid stage n      -> n words of a Stream
+//   F b v1 v2 ... (until '.')    -> exact fixed-point total of the values, as
+//                                   signed limb sums "a0 a1 a2" and the double
+//   R prec n v1..vn K s1..sK     -> sorter<prec> product (hex) and scale index
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <iostream>
+#include <sstream>
+#include <vector>
+#include "../../mixedprecisionimc.jl_gb300/csrc/imc_device.cuh"
+
+using namespace imc;
+
+int main() {
+    std::string line;
+    while (std::getline(std::cin, line)) {
+        std::istringstream in(line);
+        std::string cmd;
+        in >> cmd;
+        if (cmd == "P") {
+            uint32_t c[4], k[2], o[4];
+            in >> c[0] >> c[1] >> c[2] >> c[3] >> k[0] >> k[1];
+            philox4x32_10(c[0], c[1], c[2], c[3], k[0], k[1], o);
+            printf("%u %u %u %u\n", o[0], o[1], o[2], o[3]);
+        } else if (cmd == "S") {
+            unsigned long long seed; uint32_t step, pid, stage; int n;
+            in >> seed >> step >> pid >> stage >> n;
+            Stream s; s.init(seed, step, pid, stage);
+            for (int i = 0; i < n; ++i) printf("%u%c", s.next(), i + 1 < n ? ' ' : '\n');
+        } else if (cmd == "F") {
+            int b; in >> b;
+            long long acc[3] = {0, 0, 0};
+            std::string tok;
+            bool ok = true;
+            while (in >> tok && tok != ".") {
+                double v = strtod(tok.c_str(), nullptr);
+                Limbs L;
+                bool r = (tok.back() == 'f') ? fix_split((float)v, b, L) : fix_split(v, b, L);
+                if (!r) { ok = false; continue; }
+                acc[0] += L.l0; acc[1] += L.l1; acc[2] += L.l2;
+            }
+            printf("%d %lld %lld %lld %.17g\n", ok ? 1 : 0, acc[0], acc[1], acc[2], fix_value(acc, b));
+        } else if (cmd == "R") {
+            int prec, n, K;
+            in >> prec >> n;
+            std::vector<double> v(n);
+            for (auto &x : v) in >> x;
+            in >> K;
+            std::vector<double> s(K);
+            for (auto &x : s) in >> x;
+            int j;
+            double p = prec == 0 ? sorter<0>(v.data(), n, s.data(), K, &j)
+                     : prec == 1 ? sorter<1>(v.data(), n, s.data(), K, &j)
+                                 : sorter<2>(v.data(), n, s.data(), K, &j);
+            printf("%a %d\n", p, j);
+        }
+        fflush(stdout);
+    }
+    return 0;
+}

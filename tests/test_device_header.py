@@ -1,0 +1,96 @@
+"""The device building blocks, checked on the CPU through their host paths
+(imc_device.cuh is __host__ __device__): Philox known answers, the stream
+layout shared with the oracle, exact order-independent fixed-point tallies,
+and the sorter against the oracle's restatement."""
+import os
+import random
+import subprocess
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+
+import oracle
+
+SRC = os.path.join(REPO, "tests", "native", "device_host_check.cu")
+BIN = os.path.join(REPO, "tests", "native", "_build", "device_host_check")
+
+
+@pytest.fixture(scope="module")
+def tool():
+    os.makedirs(os.path.dirname(BIN), exist_ok=True)
+    hdr = os.path.join(REPO, "mixedprecisionimc.jl_gb300", "csrc", "imc_device.cuh")
+    if not os.path.exists(BIN) or os.path.getmtime(BIN) < max(os.path.getmtime(SRC), os.path.getmtime(hdr)):
+        nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+        subprocess.run([nvcc if os.path.exists(nvcc) else "nvcc", "-std=c++17", "-O2", "-Xcompiler",
+                        "-ffp-contract=off", SRC, "-o", BIN], check=True)
+
+    def ask(lines):
+        r = subprocess.run([BIN], input="\n".join(lines) + "\n", capture_output=True, text=True, check=True)
+        return r.stdout.strip().split("\n")
+    return ask
+
+
+def test_philox_kat_host_path(tool):
+    out = tool(["P 0 0 0 0 0 0", "P 4294967295 4294967295 4294967295 4294967295 4294967295 4294967295",
+                "P 608135816 2242054355 320440878 57701188 2752067618 698298832"])
+    assert [list(map(int, o.split())) for o in out] == [
+        [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8],
+        [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd],
+        [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]]
+
+
+def test_stream_layout_matches_oracle(tool):
+    seed, step, pid, stage = 0x123456789ABCDEF, 7, 4242, 1
+    out = list(map(int, tool(["S %d %d %d %d 9" % (seed, step, pid, stage)])[0].split()))
+    exp = []
+    for blk in range(3):
+        exp += oracle.philox([blk, step, pid, stage], [seed & 0xFFFFFFFF, seed >> 32])
+    assert out == exp[:9]
+
+
+def _exact(vals, b):
+    return sum(Fraction(v).limit_denominator(1 << 2000) if False else Fraction(v) for v in vals)
+
+
+def test_fixed_point_exact_and_order_independent(tool):
+    rng = random.Random(5)
+    vals = [rng.uniform(0, 1) * 10 ** rng.uniform(-12, 0) for _ in range(300)]
+    vals += [-rng.uniform(0, 1e-9) for _ in range(20)]  # compensation terms may be negative
+    b = -95 + 1  # exponent for vmax = 1
+    lines = []
+    for _ in range(4):
+        rng.shuffle(vals)
+        lines.append("F %d %s ." % (b, " ".join(repr(v) for v in vals)))
+    out = [o.split() for o in tool(lines)]
+    assert all(o[0] == "1" for o in out)
+    assert len({tuple(o[1:4]) for o in out}) == 1  # identical limb sums in every order
+    total = float(out[0][4])
+    exact = float(sum(Fraction(v) for v in vals))
+    # each value is rounded to 2^b once: error <= n * 2^(b-1)
+    assert abs(total - exact) <= len(vals) * 2.0 ** (b - 1) + abs(exact) * 2 ** -52
+
+
+def test_fixed_point_range_flag(tool):
+    out = tool(["F 0 1e40 ."])[0].split()
+    assert out[0] == "0"
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_sorter_matches_oracle(tool, prec):
+    rng = np.random.default_rng(prec)
+    lines, cases = [], []
+    for _ in range(40):
+        n = int(rng.integers(2, 12))
+        v = (10.0 ** rng.uniform(-6, 6, n)).tolist()
+        s = sorted((2.0 ** rng.integers(-20, 20, int(rng.integers(1, 5)))).tolist(), reverse=True)
+        lines.append("R %d %d %s %d %s" % (prec, n, " ".join(repr(x) for x in v), len(s), " ".join(repr(x) for x in s)))
+        cases.append((v, s))
+    out = tool(lines)
+    for (v, s), o in zip(cases, out):
+        p_hex, j = o.split()
+        p, _, jo = oracle.sorter(v, s, prec)
+        assert int(j) == jo
+        assert float.fromhex(p_hex) == p
