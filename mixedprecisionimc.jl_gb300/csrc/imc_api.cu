@@ -433,6 +433,12 @@ int imc_create(const ImcDeck *d, ImcHandle **out) {
     if ((rc = upload<int>(h, &ca.slot_j, nullptr, h->nslots))) return bail(rc);
     if ((rc = upload<long long>(h, &ca.slot_n, nullptr, h->nslots))) return bail(rc);
     if ((rc = upload<long long>(h, &ca.slot_off, nullptr, h->nslots))) return bail(rc);
+    if ((rc = upload<double>(h, &ca.slot_q, nullptr, h->nslots))) return bail(rc);
+    ca.nblk_slot = (h->nslots + 63) / 64;
+    ca.nblk_cell = (nc + 63) / 64;
+    if ((rc = upload<double>(h, &ca.part_src, nullptr, (size_t)ca.nblk_slot * 12))) return bail(rc);
+    if ((rc = upload<double>(h, &ca.part_emax, nullptr, (size_t)ca.nblk_slot))) return bail(rc);
+    if ((rc = upload<double>(h, &ca.part_tally, nullptr, (size_t)ca.nblk_cell * (K + 1) * 2))) return bail(rc);
     for (int b = 0; b < 4; ++b) ca.bc[b] = d->bc[b];
     ca.c = d->phys_c; ca.a = d->phys_a; ca.alpha = d->alpha; ca.ds = d->distancescale;
     ca.temp_floor = d->temp_floor; ca.cellmin = d->cellmin;
@@ -942,8 +948,8 @@ int imc_transport_timing(ImcHandle *h, double *avg_ms, int64_t *launches) {
 
 int imc_kernels_per_step(const ImcHandle *h, int *count) {
     if (!h || !count) return IMC_ERR_INVALID_ARG;
-    // update, source x3, transport, finalize, compact x4, tally, energycheck, timestep
-    *count = 13;
+    // update, source x5, transport, finalize, compact x4, tally, energycheck, timestep
+    *count = 15;
     return IMC_OK;
 }
 

@@ -33,6 +33,7 @@ struct Scalars {
     long long n_census_in;             // census carried into this step
     long long n_particles;             // list length after sourcing
     long long n_sourced;
+    double n_source;                   // particle budget of this step
     unsigned long long segments;
     unsigned long long surrogate_calls;
     unsigned int flags;
@@ -51,9 +52,14 @@ struct CellArgs {
     long long *dep_acc, *rad_acc, *lost_acc;   // 3 limbs per slot
     // sourcing scratch (per source slot)
     int nslots;
-    double *slot_e, *slot_s, *slot_nrg;
+    double *slot_e, *slot_s, *slot_nrg, *slot_q;
     int *slot_j;
     long long *slot_n, *slot_off;
+    // per-block partial sums (double-double pairs) and maxima
+    int nblk_slot, nblk_cell;          // 64-thread blocks over slots / cells
+    double *part_src;                  // [nblk_slot][6 groups][hi, lo]
+    double *part_emax;                 // [nblk_slot]
+    double *part_tally;                // [nblk_cell][K + 1][hi, lo]
     // physics / control
     int bc[4];
     double c, a, alpha, ds, temp_floor, cellmin;

@@ -2,17 +2,18 @@
 // around transport.
 //
 //   k_update           <- Update.update                 src/imc_update.jl:12-56
-//   k_source_slots     <- Sourcing.sourcing, energies     src/imc_sourcing.jl:56-121
-//   k_source_plan      <- Sourcing.sourcing, budget/counts src/imc_sourcing.jl:121-157
+//   k_source_slots     <- Sourcing.sourcing, energies     src/imc_sourcing.jl:56-111
+//   k_source_total     <- Sourcing.sourcing, total/budget src/imc_sourcing.jl:121-136
+//   k_source_counts    <- Sourcing.sourcing, counts       src/imc_sourcing.jl:138-157
 //   k_source_emit      <- Sourcing.sourcing, births        src/imc_sourcing.jl:159-366
 //   k_compact_*        <- Clean.clean                    src/imc_clean.jl:6-19
 //   k_tally            <- Tally.tally                    src/imc_tally.jl:22-142
 //   k_energycheck      <- EnergyCheck.energychecker      src/imc_energycheck.jl:19-38
 //   k_timestep         <- timestep                       src/MixedPrecisionIMC.jl:181-222
 //
-// Sums over cells are double-double per thread over a fixed assignment of
-// elements, then a fixed-order tree: deterministic, and within a rounding of
-// the exact sum.  Every launch has a fixed grid and reads its sizes from
+// Sums over cells are double-double: a fixed-order tree inside each 64-thread
+// block, then the block partials in block order -- deterministic, and within
+// a rounding of the exact sum.  Every launch has a fixed grid and reads its sizes from
 // device scalars, so a whole step can be captured once as a CUDA graph.
 #include <cstdint>
 #include "imc_device.cuh"
@@ -23,38 +24,64 @@ namespace imc {
 
 constexpr int kPlanThreads = 1024;
 
+// GB300 executes FP64 at 1/64 of the FP32 rate, so every per-cell FP64 stage
+// runs as many 64-thread blocks spread over all SMs; sums are double-double
+// per block over a fixed partition of the cells, combined in block order.
+constexpr int kCellThreads = 64;
+
+__device__ __forceinline__ DD block_reduce_dd(DD v, DD *sh) {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = kCellThreads / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            DD x = sh[threadIdx.x];
+            x.add(sh[threadIdx.x + w]);
+            sh[threadIdx.x] = x;
+        }
+        __syncthreads();
+    }
+    DD r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ DD dd_of(double x) {
+    DD d;
+    d.hi = x;
+    d.lo = 0.0;
+    return d;
+}
+
 // ------------------------------------------------------------------ update
-__global__ void k_update(CellArgs ca, Scalars *sc) {
+__global__ void __launch_bounds__(kCellThreads) k_update(CellArgs ca, Scalars *sc) {
     const double a = ca.a, c = ca.c, dt = sc->dt;
     const double one[1] = {1.0};
     if (blockIdx.x == 0 && threadIdx.x == 0) sc->flags = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ca.nc; i += gridDim.x * blockDim.x) {
-        double T = ca.temp[i];
-        double T3 = T * T * T;
-        double beta;
-        if (ca.linearized) {
-            ca.bee[i] = (4.0 * a) * T3;
-            beta = 1.0;
-        } else {
-            beta = ((4.0 * a) * T3) / ca.bee[i];
-        }
-        ca.beta[i] = beta;
-        double Tc = (ca.temp_floor > 0.0 && T < ca.temp_floor) ? ca.temp_floor : T;
-        double sa = ca.sa_val[i] * pow(Tc, ca.sa_pow[i]);
-        if (ca.marshak) sa = ca.sa_val[i] / Tc / Tc / Tc;
-        ca.sa[i] = sa;
-        ca.ss[i] = ca.ss_val[i] * pow(Tc, ca.ss_pow[i]);
-        double v[6] = {ca.ds, ca.alpha, beta, c, dt, sa};
-        int j;
-        double prod = sorter<0>(v, 6, one, 1, &j);
-        ca.fleck[i] = 1.0 / (1.0 + prod);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ca.nc) return;
+    double T = ca.temp[i];
+    double T3 = T * T * T;
+    double beta;
+    if (ca.linearized) {
+        ca.bee[i] = (4.0 * a) * T3;
+        beta = 1.0;
+    } else {
+        beta = ((4.0 * a) * T3) / ca.bee[i];
     }
+    ca.beta[i] = beta;
+    double Tc = (ca.temp_floor > 0.0 && T < ca.temp_floor) ? ca.temp_floor : T;
+    double sa = ca.sa_val[i] * pow(Tc, ca.sa_pow[i]);
+    if (ca.marshak) sa = ca.sa_val[i] / Tc / Tc / Tc;
+    ca.sa[i] = sa;
+    ca.ss[i] = ca.ss_val[i] * pow(Tc, ca.ss_pow[i]);
+    double v[6] = {ca.ds, ca.alpha, beta, c, dt, sa};
+    int j;
+    double prod = sorter<0>(v, 6, one, 1, &j);
+    ca.fleck[i] = 1.0 / (1.0 + prod);
 }
 
 void launch_update(const CellArgs &ca, Scalars *sc, cudaStream_t st) {
-    int grid = (ca.nc + 255) / 256;
-    if (grid > 1024) grid = 1024;
-    k_update<<<grid, 256, 0, st>>>(ca, sc);
+    k_update<<<ca.nblk_cell, kCellThreads, 0, st>>>(ca, sc);
 }
 
 // ---------------------------------------------------------------- sourcing
@@ -68,33 +95,44 @@ __device__ __forceinline__ int nsurf_slots(const CellArgs &ca) {
     return ca.geometry == 1 ? 2 : 2 * ca.nx + 2 * ca.ny;
 }
 
-// Energies per source slot.  Slot order is the reference's push! order:
-// 1D [left, right, body cells, source cells]; 2D [bottom x, top x, left y,
-// right y, body cells, source cells].
-__global__ void k_source_slots(CellArgs ca, Scalars *sc) {
+// source-slot groups for the energy sums: 0 body, 1 radiation source,
+// 2..5 the faces bottom, top, left, right (2D); 1D surfaces are added directly
+__device__ __forceinline__ int slot_group(const CellArgs &ca, int s) {
+    const int ns = nsurf_slots(ca);
+    if (s >= ns + ca.nc) return 1;
+    if (s >= ns) return 0;
+    if (ca.geometry == 1) return -1;
+    if (s < ca.nx) return 2;
+    if (s < 2 * ca.nx) return 3;
+    if (s < 2 * ca.nx + ca.ny) return 4;
+    return 5;
+}
+
+// Energies per source slot (src/imc_sourcing.jl:56-111).  Slot order is the
+// reference's push! order: 1D [left, right, body cells, source cells]; 2D
+// [bottom x, top x, left y, right y, body cells, source cells].  Each block
+// also leaves double-double partial sums of e/escale per slot group.
+__global__ void __launch_bounds__(kCellThreads) k_source_slots(CellArgs ca, Scalars *sc) {
+    __shared__ DD sh[kCellThreads];
     const double a = ca.a, c = ca.c, ds = ca.ds, dt = sc->dt;
     const int ns = nsurf_slots(ca), nc = ca.nc, K = ca.K;
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ca.nslots; s += gridDim.x * blockDim.x) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double q = 0.0;
+    int grp = -2;
+    if (s < ca.nslots) {
         double e = 0.0;
         int j = -1;
         if (s < ns) {
-            double Ts, w = 0.0;
-            int nv;
-            double v[9];
+            double Ts = ca.tsurf[s], w = 0.0;
             if (ca.geometry == 1) {
-                Ts = ca.tsurf[s];
-                double vv[8] = {a, c, Ts, Ts, Ts, Ts, dt, 0.25};
-                for (int q = 0; q < 8; ++q) v[q] = vv[q];
-                nv = 8;
+                double v[8] = {a, c, Ts, Ts, Ts, Ts, dt, 0.25};
+                e = sorter_sel(ca.sel_prec, v, 8, ca.scales, K, &j);
             } else {
-                Ts = ca.tsurf[s];
                 if (s < 2 * ca.nx) w = ca.dx[s % ca.nx];
                 else w = ca.dy[(s - 2 * ca.nx) % ca.ny];
-                double vv[9] = {a, c, Ts, Ts, Ts, Ts, w, dt, 0.25};
-                for (int q = 0; q < 9; ++q) v[q] = vv[q];
-                nv = 9;
+                double v[9] = {a, c, Ts, Ts, Ts, Ts, w, dt, 0.25};
+                e = sorter_sel(ca.sel_prec, v, 9, ca.scales, K, &j);
             }
-            e = sorter_sel(ca.sel_prec, v, nv, ca.scales, K, &j);
         } else if (s < ns + nc) {
             const int i = s - ns;
             const int ix = ca.geometry == 1 ? i : i % ca.nx;
@@ -111,7 +149,7 @@ __global__ void k_source_slots(CellArgs ca, Scalars *sc) {
             double ve[10] = {f, sa, a, c, T, T, T, T, dt, ds};
             int je;
             double em = sorter_sel(ca.sel_prec, ve, 10, ca.scales, K, &je);
-            for (int q = 0; q < K; ++q) ca.emitted[(size_t)q * nc + i] = 0.0;
+            for (int k = 0; k < K; ++k) ca.emitted[(size_t)k * nc + i] = 0.0;
             if (je >= 0) ca.emitted[(size_t)je * nc + i] = em;
             else atomicOr(&sc->flags, 1u << 5);
         } else {
@@ -127,100 +165,119 @@ __global__ void k_source_slots(CellArgs ca, Scalars *sc) {
             }
         }
         if (j < 0) atomicOr(&sc->flags, 1u << 5);
+        const double sv = j >= 0 ? ca.scales[j] : 0.0;
+        q = e / sv;
         ca.slot_e[s] = e;
-        ca.slot_s[s] = j >= 0 ? ca.scales[j] : 0.0;
+        ca.slot_s[s] = sv;
         ca.slot_j[s] = j;
+        ca.slot_q[s] = q;
+        grp = slot_group(ca, s);
     }
-}
-
-// deterministic block-wide double-double sum (one block)
-template <class F> __device__ double block_dd_sum(int n, F f, DD *sh) {
-    DD d;
-    d.clear();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) d.add(f(i));
-    sh[threadIdx.x] = d;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) {
-            DD x = sh[threadIdx.x];
-            x.add(sh[threadIdx.x + w]);
-            sh[threadIdx.x] = x;
+    for (int g = 0; g < 6; ++g) {
+        DD r = block_reduce_dd(dd_of(grp == g ? q : 0.0), sh);
+        if (threadIdx.x == 0) {
+            ca.part_src[(blockIdx.x * 6 + g) * 2] = r.hi;
+            ca.part_src[(blockIdx.x * 6 + g) * 2 + 1] = r.lo;
         }
-        __syncthreads();
     }
-    double r = sh[0].val();
-    __syncthreads();
-    return r;
 }
 
-__device__ __forceinline__ long long round_count(double e, double s, double n_source, double E, bool withmin,
+__device__ __forceinline__ long long round_count(double q, double n_source, double E, bool withmin,
                                                  double cellmin) {
-    double r = rint(((e / s) * n_source) / E);
+    double r = rint((q * n_source) / E);
     if (withmin) r = fmax(r, cellmin);
     return (long long)r;
 }
 
-// Budget, per-slot counts and energies, exclusive scan, fixed-point exponents.
-__global__ void __launch_bounds__(kPlanThreads) k_source_plan(CellArgs ca, Scalars *sc) {
-    __shared__ DD sh[kPlanThreads];
-    __shared__ long long warp_tot[32];
-    __shared__ long long s_run;
-    __shared__ double s_emax;
-    const int ns = nsurf_slots(ca), nc = ca.nc;
-    const double *e = ca.slot_e, *s = ca.slot_s;
-    double body = block_dd_sum(nc, [&](int i) { return e[ns + i] / s[ns + i]; }, sh);
-    double rad = block_dd_sum(nc, [&](int i) { return e[ns + nc + i] / s[ns + nc + i]; }, sh);
+// Total energy (src/imc_sourcing.jl:121) and particle budget (:132-136).
+__global__ void k_source_total(CellArgs ca, Scalars *sc) {
+    if (threadIdx.x != 0) return;
+    const int nb = ca.nblk_slot;
+    double g[6];
+    for (int k = 0; k < 6; ++k) {
+        DD d;
+        d.clear();
+        for (int bb = 0; bb < nb; ++bb) {
+            DD p;
+            p.hi = ca.part_src[(bb * 6 + k) * 2];
+            p.lo = ca.part_src[(bb * 6 + k) * 2 + 1];
+            d.add(p);
+        }
+        g[k] = d.val();
+    }
     double e_surface;
     if (ca.geometry == 1) {
-        e_surface = (e[0] / s[0]) + (e[1] / s[1]);
+        e_surface = ca.slot_q[0] + ca.slot_q[1];
     } else {
-        const int nx = ca.nx, ny = ca.ny;
         e_surface = 0.0;
-        e_surface += block_dd_sum(nx, [&](int i) { return e[i] / s[i]; }, sh);
-        e_surface += block_dd_sum(nx, [&](int i) { return e[nx + i] / s[nx + i]; }, sh);
-        e_surface += block_dd_sum(ny, [&](int i) { return e[2 * nx + i] / s[2 * nx + i]; }, sh);
-        e_surface += block_dd_sum(ny, [&](int i) { return e[2 * nx + ny + i] / s[2 * nx + ny + i]; }, sh);
+        e_surface += g[2];
+        e_surface += g[3];
+        e_surface += g[4];
+        e_surface += g[5];
     }
-    const double E = body + rad + e_surface;
+    const double E = g[0] + g[1] + e_surface;
     const long long n_census = sc->n_census;
     double n_source = (double)ca.n_input;
     if (ca.n_input + n_census > ca.n_max) {
         double lenN = ca.geometry == 1 ? 1.0 : 2.0;
         n_source = fmax(ca.cellmin, (double)(ca.n_max - n_census) - lenN - 1.0);
     }
+    sc->totalenergy = E;
+    sc->n_source = n_source;
+    if (!((E > 0.0) && isfinite(E))) sc->flags |= 1u << 4;
+}
+
+// Births per slot (src/imc_sourcing.jl:138-157) and per-particle energy.
+__global__ void __launch_bounds__(kCellThreads) k_source_counts(CellArgs ca, Scalars *sc) {
+    __shared__ double wm[kCellThreads / 32];
+    const int ns = nsurf_slots(ca), nc = ca.nc;
+    const double E = sc->totalenergy, n_source = sc->n_source;
     const bool ok = (E > 0.0) && isfinite(E);
-    const bool surf_min = ca.geometry == 2;
-    // counts and per-particle energies
-    for (int q = threadIdx.x; q < ca.nslots; q += blockDim.x) {
-        long long n = 0;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    double my = 0.0;
+    if (q < ca.nslots) {
+        const double *e = ca.slot_e, *qv = ca.slot_q;
+        long long n = 0, nd = 0;
         if (ok) {
             if (q < ns) {
-                if (e[q] > 0) n = round_count(e[q], s[q], n_source, E, surf_min, ca.cellmin);
+                if (e[q] > 0) n = round_count(qv[q], n_source, E, ca.geometry == 2, ca.cellmin);
+                nd = n;
             } else if (q < ns + nc) {
-                n = round_count(e[q], s[q], n_source, E, true, ca.cellmin);
-            } else {
-                if (e[q] > 0) {
-                    n = round_count(e[q], s[q], n_source, E, true, ca.cellmin);
-                    // 2D births n_body particles per source cell (src/imc_sourcing.jl:357)
-                    if (ca.geometry == 2 && n > 0)
-                        n = round_count(e[q - nc], s[q - nc], n_source, E, true, ca.cellmin);
-                }
+                n = round_count(qv[q], n_source, E, true, ca.cellmin);
+                nd = n;
+            } else if (e[q] > 0) {
+                n = round_count(qv[q], n_source, E, true, ca.cellmin);
+                nd = n;
+                // 2D births n_body particles per source cell (src/imc_sourcing.jl:357)
+                if (ca.geometry == 2 && n > 0) n = round_count(qv[q - nc], n_source, E, true, ca.cellmin);
             }
             if (n < 0) n = 0;
         }
-        double nrg = 0.0;
-        if (n > 0) {
-            long long nd = n;
-            if (ca.geometry == 2 && q >= ns + nc) nd = round_count(e[q], s[q], n_source, E, true, ca.cellmin);
-            nrg = e[q] / (double)nd;
-        }
+        const double nrg = n > 0 ? e[q] / (double)nd : 0.0;
         ca.slot_n[q] = n;
         ca.slot_nrg[q] = nrg;
+        if (n > 0) my = nrg;
     }
-    if (threadIdx.x == 0) { s_run = 0; s_emax = 0.0; }
+    for (int off = 16; off > 0; off >>= 1) {
+        double o = __shfl_down_sync(0xFFFFFFFFu, my, off);
+        my = o > my ? o : my;
+    }
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = my;
     __syncthreads();
-    // exclusive scan of slot_n, chunked
+    if (threadIdx.x == 0) {
+        double m = wm[0];
+        for (int w = 1; w < kCellThreads / 32; ++w) m = wm[w] > m ? wm[w] : m;
+        ca.part_emax[blockIdx.x] = m;
+    }
+}
+
+// Exclusive scan of the births, capacity check, fixed-point exponents.
+__global__ void __launch_bounds__(kPlanThreads) k_source_scan(CellArgs ca, Scalars *sc) {
+    __shared__ long long warp_tot[32];
+    __shared__ long long s_run;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_run = 0;
+    __syncthreads();
     for (int base = 0; base < ca.nslots; base += blockDim.x) {
         int q = base + threadIdx.x;
         long long v = q < ca.nslots ? ca.slot_n[q] : 0;
@@ -246,31 +303,17 @@ __global__ void __launch_bounds__(kPlanThreads) k_source_plan(CellArgs ca, Scala
         if (threadIdx.x == blockDim.x - 1) s_run = excl + v;
         __syncthreads();
     }
-    // largest per-particle energy of this step's births
-    double my = 0.0;
-    for (int q = threadIdx.x; q < ca.nslots; q += blockDim.x)
-        if (ca.slot_n[q] > 0 && ca.slot_nrg[q] > my) my = ca.slot_nrg[q];
-    for (int off = 16; off > 0; off >>= 1) {
-        double o = __shfl_down_sync(0xFFFFFFFFu, my, off);
-        my = o > my ? o : my;
-    }
-    if (lane == 0) {
-        unsigned long long bits = (unsigned long long)d2u(my);
-        atomicMax((unsigned long long *)&s_emax, bits);
-    }
-    __syncthreads();
     if (threadIdx.x == 0) {
+        const long long n_census = sc->n_census;
         long long n_new = s_run;
         unsigned fl = 0;
-        if (!ok) fl |= 1u << 4;
         if (n_census + n_new > ca.capacity) {
             n_new = ca.capacity - n_census;
             if (n_new < 0) n_new = 0;
             fl |= 1u << 3;
         }
-        double emax_c = __longlong_as_double((long long)sc->emax_census_bits);
-        double emax = fmax(emax_c, s_emax);
-        sc->totalenergy = E;
+        double emax = __longlong_as_double((long long)sc->emax_census_bits);
+        for (int bb = 0; bb < ca.nblk_slot; ++bb) emax = fmax(emax, ca.part_emax[bb]);
         sc->n_census_in = n_census;
         sc->n_sourced = n_new;
         sc->n_particles = n_census + n_new;
@@ -420,10 +463,11 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
 }
 
 void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, cudaStream_t st) {
-    int g = (ca.nslots + 255) / 256;
-    if (g > 1024) g = 1024;
-    k_source_slots<<<g, 256, 0, st>>>(ca, sc);
-    k_source_plan<<<1, kPlanThreads, 0, st>>>(ca, sc);
+    const int nb = ca.nblk_slot;
+    k_source_slots<<<nb, kCellThreads, 0, st>>>(ca, sc);
+    k_source_total<<<1, 32, 0, st>>>(ca, sc);
+    k_source_counts<<<nb, kCellThreads, 0, st>>>(ca, sc);
+    k_source_scan<<<1, kPlanThreads, 0, st>>>(ca, sc);
     if (prec == 0) k_source_emit<StF64><<<grid, 256, 0, st>>>(ca, sc, buf);
     else if (prec == 1) k_source_emit<StF32><<<grid, 256, 0, st>>>(ca, sc, buf);
     else k_source_emit<StF16><<<grid, 256, 0, st>>>(ca, sc, buf);
@@ -560,25 +604,25 @@ __device__ __forceinline__ double cell_vol(const CellArgs &ca, int i) {
 // clears the accumulators: energydep and the escaped energy as
 // Transport.MC leaves them (src/imc_transport.jl:198-205), and the census
 // radiation energy density of src/imc_tally.jl:81-113.
-__global__ void __launch_bounds__(kPlanThreads) k_finalize(CellArgs ca, Scalars *sc) {
+__global__ void __launch_bounds__(kCellThreads) k_finalize(CellArgs ca, Scalars *sc) {
     const int nc = ca.nc, K = ca.K;
     const int b_dep = sc->b_dep, b_rad = sc->b_rad, b_lost = sc->b_lost;
-    for (int idx = threadIdx.x; idx < K * nc; idx += blockDim.x) {
-        long long *d = ca.dep_acc + 3 * (size_t)idx;
-        ca.energydep[idx] = fix_value(d, b_dep);
-        d[0] = d[1] = d[2] = 0;
-    }
-    for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nc) {
         const double vol = cell_vol(ca, i);
         double r = 0.0;
         for (int k = 0; k < K; ++k) {
-            long long *d = ca.rad_acc + 3 * ((size_t)k * nc + i);
-            r += fix_value(d, b_rad) / (vol * ca.scales[k]);
+            const size_t idx = (size_t)k * nc + i;
+            long long *d = ca.dep_acc + 3 * idx;
+            ca.energydep[idx] = fix_value(d, b_dep);
             d[0] = d[1] = d[2] = 0;
+            long long *g = ca.rad_acc + 3 * idx;
+            r += fix_value(g, b_rad) / (vol * ca.scales[k]);
+            g[0] = g[1] = g[2] = 0;
         }
         ca.radenergydens[i] = r;
     }
-    if (threadIdx.x == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         double lost = 0.0;
         for (int k = 0; k < K; ++k) {
             long long *d = ca.lost_acc + 3 * k;
@@ -590,15 +634,22 @@ __global__ void __launch_bounds__(kPlanThreads) k_finalize(CellArgs ca, Scalars 
     }
 }
 
-void launch_finalize(const CellArgs &ca, Scalars *sc, cudaStream_t st) { k_finalize<<<1, kPlanThreads, 0, st>>>(ca, sc); }
+void launch_finalize(const CellArgs &ca, Scalars *sc, cudaStream_t st) {
+    k_finalize<<<ca.nblk_cell, kCellThreads, 0, st>>>(ca, sc);
+}
 
-__global__ void __launch_bounds__(kPlanThreads) k_tally(CellArgs ca, Scalars *sc) {
-    __shared__ DD sh[kPlanThreads];
+// Tally.tally per cell (src/imc_tally.jl:29-75); each block leaves partial
+// sums of the deposited energy per scale and of the radiation energy.
+__global__ void __launch_bounds__(kCellThreads) k_tally(CellArgs ca, Scalars *sc) {
+    __shared__ DD sh[kCellThreads];
     const int nc = ca.nc, K = ca.K;
     const double a = ca.a, c = ca.c, dt = sc->dt;
     const bool first = sc->t == 0.0;
     const double one[1] = {1.0};
-    for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double vol = 0.0;
+    if (i < nc) {
+        vol = cell_vol(ca, i);
         if (first) {
             double T = ca.temp[i];
             double v[10] = {ca.fleck[i], ca.sa[i], a, c, T, T, T, T, dt, ca.ds};
@@ -613,49 +664,70 @@ __global__ void __launch_bounds__(kPlanThreads) k_tally(CellArgs ca, Scalars *sc
         if (ca.linearized) ca.temp[i] = pow(m, 0.25);
         else ca.temp[i] = ca.temp[i] + inc / ca.bee[i];
     }
-    double totdep = 0.0;
+    const int np = K + 1;
     for (int k = 0; k < K; ++k) {
-        const double sk = ca.scales[k];
-        totdep += block_dd_sum(nc, [&](int i) { return (ca.energydep[(size_t)k * nc + i] * cell_vol(ca, i)) / sk; }, sh);
+        double x = i < nc ? (ca.energydep[(size_t)k * nc + i] * vol) / ca.scales[k] : 0.0;
+        DD r = block_reduce_dd(dd_of(x), sh);
+        if (threadIdx.x == 0) {
+            ca.part_tally[(blockIdx.x * np + k) * 2] = r.hi;
+            ca.part_tally[(blockIdx.x * np + k) * 2 + 1] = r.lo;
+        }
     }
-    if (threadIdx.x == 0) sc->totalenergydep = totdep;
+    DD r = block_reduce_dd(dd_of(i < nc ? ca.radenergydens[i] * vol : 0.0), sh);
+    if (threadIdx.x == 0) {
+        ca.part_tally[(blockIdx.x * np + K) * 2] = r.hi;
+        ca.part_tally[(blockIdx.x * np + K) * 2 + 1] = r.lo;
+    }
 }
 
-void launch_tally(const CellArgs &ca, Scalars *sc, cudaStream_t st) { k_tally<<<1, kPlanThreads, 0, st>>>(ca, sc); }
+void launch_tally(const CellArgs &ca, Scalars *sc, cudaStream_t st) {
+    k_tally<<<ca.nblk_cell, kCellThreads, 0, st>>>(ca, sc);
+}
 
-__global__ void __launch_bounds__(kPlanThreads) k_energycheck(CellArgs ca, Scalars *sc, DevStats *stats,
-                                                              long long stats_cap) {
-    __shared__ DD sh[kPlanThreads];
-    double radenergy = block_dd_sum(ca.nc, [&](int i) { return ca.radenergydens[i] * cell_vol(ca, i); }, sh);
-    if (threadIdx.x == 0) {
-        double err = (sc->totalenergy - sc->totalenergydep - (radenergy - sc->radenergyold) - sc->lostenergy) /
-                     sc->totalenergy;
-        if (stats && stats_cap > 0) {
-            DevStats &d = stats[sc->step % (unsigned long long)stats_cap];
-            d.t = sc->t; d.dt = sc->dt;
-            d.total_energy = sc->totalenergy;
-            d.energy_dep = sc->totalenergydep;
-            d.rad_energy = radenergy;
-            d.rad_energy_old = sc->radenergyold;
-            d.lost_energy = sc->lostenergy;
-            d.energy_error = err;
-            d.n_census_in = sc->n_census_in;
-            d.n_sourced = sc->n_sourced;
-            d.n_census_out = sc->n_census;
-            d.segments = (long long)sc->segments;
-            d.surrogate_calls = (long long)sc->surrogate_calls;
-            d.error_flags = sc->flags;
-            d.step_index = sc->step;
+// EnergyCheck.energychecker (src/imc_energycheck.jl:19-38).
+__global__ void k_energycheck(CellArgs ca, Scalars *sc, DevStats *stats, long long stats_cap) {
+    if (threadIdx.x != 0) return;
+    const int np = ca.K + 1, nb = ca.nblk_cell;
+    double totdep = 0.0, radenergy = 0.0;
+    for (int k = 0; k <= ca.K; ++k) {
+        DD d;
+        d.clear();
+        for (int bb = 0; bb < nb; ++bb) {
+            DD p;
+            p.hi = ca.part_tally[(bb * np + k) * 2];
+            p.lo = ca.part_tally[(bb * np + k) * 2 + 1];
+            d.add(p);
         }
-        sc->energy_err = err;
-        sc->radenergy = radenergy;
-        sc->radenergyold = radenergy;
-        sc->lostenergy = 0.0;
+        if (k < ca.K) totdep += d.val();
+        else radenergy = d.val();
     }
+    sc->totalenergydep = totdep;
+    double err = (sc->totalenergy - totdep - (radenergy - sc->radenergyold) - sc->lostenergy) / sc->totalenergy;
+    if (stats && stats_cap > 0) {
+        DevStats &d = stats[sc->step % (unsigned long long)stats_cap];
+        d.t = sc->t; d.dt = sc->dt;
+        d.total_energy = sc->totalenergy;
+        d.energy_dep = totdep;
+        d.rad_energy = radenergy;
+        d.rad_energy_old = sc->radenergyold;
+        d.lost_energy = sc->lostenergy;
+        d.energy_error = err;
+        d.n_census_in = sc->n_census_in;
+        d.n_sourced = sc->n_sourced;
+        d.n_census_out = sc->n_census;
+        d.segments = (long long)sc->segments;
+        d.surrogate_calls = (long long)sc->surrogate_calls;
+        d.error_flags = sc->flags;
+        d.step_index = sc->step;
+    }
+    sc->energy_err = err;
+    sc->radenergy = radenergy;
+    sc->radenergyold = radenergy;
+    sc->lostenergy = 0.0;
 }
 
 void launch_energycheck(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap, cudaStream_t st) {
-    k_energycheck<<<1, kPlanThreads, 0, st>>>(ca, sc, stats, stats_cap);
+    k_energycheck<<<1, 32, 0, st>>>(ca, sc, stats, stats_cap);
 }
 
 // timestep (src/MixedPrecisionIMC.jl:181-222), FP64 on the device so a run
