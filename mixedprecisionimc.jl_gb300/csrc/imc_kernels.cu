@@ -174,6 +174,14 @@ __global__ void __launch_bounds__(kCellThreads) k_source_slots(CellArgs ca, Scal
         grp = slot_group(ca, s);
     }
     for (int g = 0; g < 6; ++g) {
+        // most blocks hold one group: reduce only the groups present
+        if (!__syncthreads_or(grp == g)) {
+            if (threadIdx.x == 0) {
+                ca.part_src[(blockIdx.x * 6 + g) * 2] = 0.0;
+                ca.part_src[(blockIdx.x * 6 + g) * 2 + 1] = 0.0;
+            }
+            continue;
+        }
         DD r = block_reduce_dd(dd_of(grp == g ? q : 0.0), sh);
         if (threadIdx.x == 0) {
             ca.part_src[(blockIdx.x * 6 + g) * 2] = r.hi;
@@ -189,22 +197,36 @@ __device__ __forceinline__ long long round_count(double q, double n_source, doub
     return (long long)r;
 }
 
-// Total energy (src/imc_sourcing.jl:121) and particle budget (:132-136).
-__global__ void k_source_total(CellArgs ca, Scalars *sc) {
-    if (threadIdx.x != 0) return;
-    const int nb = ca.nblk_slot;
-    double g[6];
-    for (int k = 0; k < 6; ++k) {
-        DD d;
-        d.clear();
-        for (int bb = 0; bb < nb; ++bb) {
-            DD p;
-            p.hi = ca.part_src[(bb * 6 + k) * 2];
-            p.lo = ca.part_src[(bb * 6 + k) * 2 + 1];
-            d.add(p);
-        }
-        g[k] = d.val();
+// Sum of the double-double block partials of one group by one warp: lane l
+// takes blocks l, l+32, ..., then a fixed shuffle tree.  Deterministic.
+__device__ __forceinline__ double warp_sum_partials(const double *part, int nb, int stride, int g) {
+    const int lane = threadIdx.x & 31;
+    DD d;
+    d.clear();
+    for (int bb = lane; bb < nb; bb += 32) {
+        DD p;
+        p.hi = part[(bb * stride + g) * 2];
+        p.lo = part[(bb * stride + g) * 2 + 1];
+        d.add(p);
     }
+    for (int off = 16; off > 0; off >>= 1) {
+        DD o;
+        o.hi = __shfl_down_sync(0xFFFFFFFFu, d.hi, off);
+        o.lo = __shfl_down_sync(0xFFFFFFFFu, d.lo, off);
+        if (lane < off) d.add(o);
+    }
+    return __shfl_sync(0xFFFFFFFFu, d.val(), 0);
+}
+
+// Total energy (src/imc_sourcing.jl:121) and particle budget (:132-136).
+// Six warps, one per slot group.
+__global__ void __launch_bounds__(192) k_source_total(CellArgs ca, Scalars *sc) {
+    __shared__ double g[6];
+    const int warp = threadIdx.x >> 5;
+    double v = warp_sum_partials(ca.part_src, ca.nblk_slot, 6, warp);
+    if ((threadIdx.x & 31) == 0) g[warp] = v;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     double e_surface;
     if (ca.geometry == 1) {
         e_surface = ca.slot_q[0] + ca.slot_q[1];
@@ -465,7 +487,7 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
 void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, cudaStream_t st) {
     const int nb = ca.nblk_slot;
     k_source_slots<<<nb, kCellThreads, 0, st>>>(ca, sc);
-    k_source_total<<<1, 32, 0, st>>>(ca, sc);
+    k_source_total<<<1, 192, 0, st>>>(ca, sc);
     k_source_counts<<<nb, kCellThreads, 0, st>>>(ca, sc);
     k_source_scan<<<1, kPlanThreads, 0, st>>>(ca, sc);
     if (prec == 0) k_source_emit<StF64><<<grid, 256, 0, st>>>(ca, sc, buf);
@@ -537,45 +559,65 @@ __global__ void __launch_bounds__(1024) k_compact_scan(Scalars *sc, const long l
     }
 }
 
+// Copies one field of a tile: coalesced load of the tile into shared memory,
+// then coalesced stores of the survivors in order (src_idx[j] is the tile
+// position of the j-th survivor).
+template <class V>
+__device__ __forceinline__ void scatter_field(const V *src, V *dst, long long base, int tile_n, long long out,
+                                              int cnt, const unsigned short *src_idx, unsigned char *stage) {
+    V *st = reinterpret_cast<V *>(stage);
+    for (int i = threadIdx.x; i < tile_n; i += blockDim.x) st[i] = src[base + i];
+    __syncthreads();
+    for (int j = threadIdx.x; j < cnt; j += blockDim.x) dst[out + j] = st[src_idx[j]];
+    __syncthreads();
+}
+
 template <class St>
 __global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(int geometry, const Scalars *sc,
                                                                      const long long *tile_off, PBufRaw sraw,
                                                                      PBufRaw draw, const long long *n_before) {
     PBuf<St> src(sraw), dst(draw);
+    __shared__ unsigned short src_idx[kCompactTile];
+    __shared__ __align__(16) unsigned char stage[kCompactTile * 8];
+    __shared__ int wt[kCompactThreads / 32];
+    __shared__ int s_tot;
     const long long n = *n_before;
     const long long base = (long long)blockIdx.x * kCompactTile;
     if (base >= n) return;
-    __shared__ int wt[kCompactThreads / 32];
-    __shared__ int s_tot;
+    const int tile_n = (int)((n - base) < kCompactTile ? (n - base) : kCompactTile);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    long long run = tile_off[blockIdx.x];
+    // survivor list of the tile, in order
+    int run = 0;
     for (int r = 0; r < kCompactTile; r += kCompactThreads) {
-        const long long i = base + r + threadIdx.x;
-        const bool f = i < n && src.alive[i];
+        const int i = r + threadIdx.x;
+        const bool f = i < tile_n && src.alive[base + i];
         const unsigned m = __ballot_sync(0xFFFFFFFFu, f);
         const int wpre = __popc(m & ((1u << lane) - 1u));
         if (lane == 0) wt[warp] = __popc(m);
         __syncthreads();
         if (threadIdx.x == 0) {
-            int s = 0;
-            for (int w = 0; w < kCompactThreads / 32; ++w) { int v = wt[w]; wt[w] = s; s += v; }
-            s_tot = s;
+            int acc = 0;
+            for (int w = 0; w < kCompactThreads / 32; ++w) { int v = wt[w]; wt[w] = acc; acc += v; }
+            s_tot = acc;
         }
         __syncthreads();
-        if (f) {
-            const long long d = run + wt[warp] + wpre;
-            dst.t[d] = src.t[i];
-            dst.x[d] = src.x[i];
-            dst.ux[d] = src.ux[i];
-            if (geometry == 2) { dst.y[d] = src.y[i]; dst.uy[d] = src.uy[i]; }
-            dst.E[d] = src.E[i];
-            dst.E0[d] = src.E0[i];
-            dst.cs[d] = src.cs[i];
-            dst.alive[d] = 1;
-        }
+        if (f) src_idx[run + wt[warp] + wpre] = (unsigned short)i;
         run += s_tot;
         __syncthreads();
     }
+    const int cnt = run;
+    const long long out = tile_off[blockIdx.x];
+    scatter_field(src.t, dst.t, base, tile_n, out, cnt, src_idx, stage);
+    scatter_field(src.x, dst.x, base, tile_n, out, cnt, src_idx, stage);
+    scatter_field(src.ux, dst.ux, base, tile_n, out, cnt, src_idx, stage);
+    if (geometry == 2) {
+        scatter_field(src.y, dst.y, base, tile_n, out, cnt, src_idx, stage);
+        scatter_field(src.uy, dst.uy, base, tile_n, out, cnt, src_idx, stage);
+    }
+    scatter_field(src.E, dst.E, base, tile_n, out, cnt, src_idx, stage);
+    scatter_field(src.E0, dst.E0, base, tile_n, out, cnt, src_idx, stage);
+    scatter_field(src.cs, dst.cs, base, tile_n, out, cnt, src_idx, stage);
+    for (int j = threadIdx.x; j < cnt; j += blockDim.x) dst.alive[out + j] = 1;
 }
 
 __global__ void k_copy_count(const Scalars *sc, long long *n_before) { *n_before = sc->n_particles; }
@@ -684,23 +726,20 @@ void launch_tally(const CellArgs &ca, Scalars *sc, cudaStream_t st) {
     k_tally<<<ca.nblk_cell, kCellThreads, 0, st>>>(ca, sc);
 }
 
-// EnergyCheck.energychecker (src/imc_energycheck.jl:19-38).
-__global__ void k_energycheck(CellArgs ca, Scalars *sc, DevStats *stats, long long stats_cap) {
-    if (threadIdx.x != 0) return;
-    const int np = ca.K + 1, nb = ca.nblk_cell;
-    double totdep = 0.0, radenergy = 0.0;
-    for (int k = 0; k <= ca.K; ++k) {
-        DD d;
-        d.clear();
-        for (int bb = 0; bb < nb; ++bb) {
-            DD p;
-            p.hi = ca.part_tally[(bb * np + k) * 2];
-            p.lo = ca.part_tally[(bb * np + k) * 2 + 1];
-            d.add(p);
-        }
-        if (k < ca.K) totdep += d.val();
-        else radenergy = d.val();
+// EnergyCheck.energychecker (src/imc_energycheck.jl:19-38).  One warp per
+// partial-sum group (K deposition scales, then the radiation energy).
+__global__ void __launch_bounds__(544) k_energycheck(CellArgs ca, Scalars *sc, DevStats *stats, long long stats_cap) {
+    __shared__ double g[17];
+    const int warp = threadIdx.x >> 5, np = ca.K + 1;
+    if (warp < np) {
+        double v = warp_sum_partials(ca.part_tally, ca.nblk_cell, np, warp);
+        if ((threadIdx.x & 31) == 0) g[warp] = v;
     }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    double totdep = 0.0;
+    for (int k = 0; k < ca.K; ++k) totdep += g[k];
+    const double radenergy = g[ca.K];
     sc->totalenergydep = totdep;
     double err = (sc->totalenergy - totdep - (radenergy - sc->radenergyold) - sc->lostenergy) / sc->totalenergy;
     if (stats && stats_cap > 0) {
@@ -727,7 +766,7 @@ __global__ void k_energycheck(CellArgs ca, Scalars *sc, DevStats *stats, long lo
 }
 
 void launch_energycheck(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap, cudaStream_t st) {
-    k_energycheck<<<1, 32, 0, st>>>(ca, sc, stats, stats_cap);
+    k_energycheck<<<1, 32 * (ca.K + 1), 0, st>>>(ca, sc, stats, stats_cap);
 }
 
 // timestep (src/MixedPrecisionIMC.jl:181-222), FP64 on the device so a run

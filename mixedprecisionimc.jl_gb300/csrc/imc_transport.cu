@@ -81,17 +81,16 @@ __device__ __forceinline__ void flush_block_tallies(const CellArgs &ca, const lo
     }
 }
 
-// flush a compensated pair (s, c) into accumulator slot
+// flush a compensated pair: the Neumaier result s + c, converted once
 template <class T, bool SMT>
 __device__ __forceinline__ void flush_pair(long long *acc, int slot, T s, T c, int b, unsigned &flags) {
-    if (s == (T)0 && c == (T)0) return;
-    Limbs A, B;
-    bool ok = fix_split(s, b, A) && fix_split(c, b, B);
-    if (!ok) {
-        flags |= (s != s || c != c) ? 1u /*NAN*/ : (1u << 5) /*FIXPOINT_RANGE*/;
+    const T v = s + c;
+    if (v == (T)0) return;
+    Limbs A;
+    if (!fix_split(v, b, A)) {
+        flags |= (v != v) ? 1u /*NAN*/ : (1u << 5) /*FIXPOINT_RANGE*/;
         return;
     }
-    A.l0 += B.l0; A.l1 += B.l1; A.l2 += B.l2;
     add_limbs<SMT>(acc + 3 * (size_t)slot, A);
 }
 
@@ -136,6 +135,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     Tab1<T> *tab = reinterpret_cast<Tab1<T> *>(smem_raw);
     const int N = ca.nx;
     const T ds = (T)ca.ds, c = (T)ca.c;
+    const bool ds_one = ds == (T)1;
     long long *dep_acc = ca.dep_acc, *rad_acc = ca.rad_acc;
     if (SMT) {
         dep_acc = tally_smem(smem_raw, table_bytes(ca, sizeof(T)));
@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
             }
             nadd(acc_s, acc_c, -(E / ce.dxT) * m_expm1(-ce.saf * dist));
             x += mu * dist;
-            t += (dist / ds) / c;
+            t += (ds_one ? dist : dist / ds) / c;
             E = newenergy;
             if (dist == dist_b) {
                 if (mu > (T)0) {
@@ -284,6 +284,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
     Face<T> *fx = reinterpret_cast<Face<T> *>(tab + nc);
     Face<T> *fy = fx + NX;
     const T ds = (T)ca.ds, c = (T)ca.c;
+    const bool ds_one = ds == (T)1;
     long long *dep_acc = ca.dep_acc, *rad_acc = ca.rad_acc;
     if (SMT) {
         dep_acc = tally_smem(smem_raw, table_bytes(ca, sizeof(T)));
@@ -365,7 +366,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
             nadd(acc_s, acc_c, -Edens * m_expm1(-ce.saf * dist));
             xp += dist * vx;
             yp += dist * vy;
-            t += (dist / ds) / c;
+            t += (ds_one ? dist : dist / ds) / c;
             E = newenergy;
             if (dist == dist_bx || dist == dist_by) {
                 if (dist_bx < dist_by) {

@@ -1,0 +1,48 @@
+"""Statistical agreement with the FP64 oracle: ensemble means over 32 seeds of
+the final cell temperature and radiation energy density on the C1 slab,
+within 3 sigma, for every particle-state precision of the GPU engine.  The
+oracle ensemble is the committed fixture tests/golden/c1_oracle_fp64_32seeds.npz
+(tests/golden/make_c1_golden.py); the GPU runs use disjoint seeds."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import REPO, load_deck
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(REPO, "tests", "golden", "c1_oracle_fp64_32seeds.npz")
+
+
+def _ensemble(prec, seeds):
+    import mpimc
+    T, R = [], []
+    for sd in seeds:
+        inputs, mesh = load_deck("c1_slab", PRECISION=prec, SEED=str(sd))
+        e = mpimc.Engine(inputs, mesh)
+        steps, _ = e.run()
+        assert len(steps) == 101
+        assert all(s["error_flags"] == 0 for s in steps)
+        T.append(e.field("temp"))
+        R.append(e.field("radenergydens"))
+        e.close()
+    return np.array(T), np.array(R)
+
+
+def _z(gpu, mean_o, std_o, n_o):
+    m, s = gpu.mean(0), gpu.std(0, ddof=1)
+    return (m - mean_o) / np.sqrt(s ** 2 / len(gpu) + std_o ** 2 / n_o)
+
+
+@pytest.mark.parametrize("prec", [np.float64, np.float32, np.float16])
+def test_c1_ensemble_within_3_sigma(prec, gpu_lib):
+    g = np.load(GOLD)
+    n_o = len(g["seeds"])
+    T, R = _ensemble(prec, [900 + i for i in range(32)])
+    for name, arr, mo, so in (("temp", T, g["temp_mean"], g["temp_std"]), ("rad", R, g["rad_mean"], g["rad_std"])):
+        live = so > 0
+        z = _z(arr[:, live], mo[live], so[live], n_o)
+        # 100 cells: allow the odd 3-sigma excursion, bound the chi-square
+        assert np.mean(np.abs(z) < 3.0) >= 0.97, (name, np.sort(np.abs(z))[-5:])
+        assert np.mean(z ** 2) < 1.0 + 6.0 * np.sqrt(2.0 / live.sum()), (name, np.mean(z ** 2))
