@@ -249,6 +249,35 @@ int imc_transport_timing(ImcHandle *h, double *avg_ms, int64_t *launches);
 /* Number of kernel launches one step issues (for launch accounting). */
 int imc_kernels_per_step(const ImcHandle *h, int *count);
 
+/* ---- compaction for callers that cannot allocate ------------------------ */
+
+/* Device-resident particle arrays owned by the caller (structure of arrays,
+ * element type by precision: double / float / binary16 state, double or
+ * float E0).  1D uses t, x, ux (mu), E, E0; 2D also y, uy.  cs = cell |
+ * scale_index << 24; alive = 1 byte per particle. */
+typedef struct ImcDeviceParticles {
+    void *t, *x, *y, *ux, *uy, *E, *E0;
+    int32_t *cs;
+    uint8_t *alive;
+} ImcDeviceParticles;
+
+/* No counterpart in the reference.  Stable removal of the particles whose
+ * alive byte is 0 -- the compaction imc_clean performs -- from caller-owned
+ * device arrays `src` into caller-owned `dst`, for callers that cannot call
+ * cudaMalloc: work enqueued during a CUDA stream capture, hosts whose device
+ * memory belongs to their own pool allocator, loops that cannot take the
+ * device-wide synchronisation of an allocation.  It allocates nothing: its
+ * scratch is a fixed 72 KiB __device__ array that every GPU loading the
+ * library holds until exit, which limits n to 16,777,216 particles (larger n
+ * returns IMC_ERR_INVALID_ARG).  The first call on a device looks the array's
+ * address up with that device current; make it before any stream capture.
+ * All calls share the array, so calls that overlap on the GPU race.  Work is
+ * ordered on `stream` (a cudaStream_t; NULL = the default stream); the call
+ * returns once *n_out, the number of survivors, is known.
+ * Returns IMC_OK, IMC_ERR_INVALID_ARG, IMC_ERR_NO_DEVICE or IMC_ERR_CUDA. */
+int imc_clean_noalloc(int precision, int geometry, const ImcDeviceParticles *src, ImcDeviceParticles *dst,
+                      int64_t n, int64_t *n_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

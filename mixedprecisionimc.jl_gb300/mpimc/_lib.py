@@ -99,6 +99,12 @@ class ImcParticles(C.Structure):
     ]
 
 
+class ImcDeviceParticles(C.Structure):
+    """Caller-owned device arrays for imc_clean_noalloc (device pointers)."""
+    _fields_ = [("t", C.c_void_p), ("x", C.c_void_p), ("y", C.c_void_p), ("ux", C.c_void_p), ("uy", C.c_void_p),
+                ("E", C.c_void_p), ("E0", C.c_void_p), ("cs", C.c_void_p), ("alive", C.c_void_p)]
+
+
 class ImcError(RuntimeError):
     def __init__(self, code, msg):
         self.code = code
@@ -133,6 +139,8 @@ SIGNATURES = {
     "imc_set_timing": (C.c_int, [_H, C.c_int]),
     "imc_transport_timing": (C.c_int, [_H, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "imc_kernels_per_step": (C.c_int, [_H, C.POINTER(C.c_int)]),
+    "imc_clean_noalloc": (C.c_int, [C.c_int, C.c_int, C.POINTER(ImcDeviceParticles), C.POINTER(ImcDeviceParticles),
+                                    C.c_int64, C.POINTER(C.c_int64), C.c_void_p]),
 }
 
 _LIB = None
