@@ -35,16 +35,41 @@ import time
 
 REPO = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(REPO, "mixedprecisionimc.jl_gb300")
-DECK = os.path.join(REPO, "tests", "golden", "decks", "c2_slab_fine.txt")
-REF_MEAN = os.path.join(REPO, "tests", "golden", "c2_fp64_mean.npz")
+GOLDEN = os.path.join(REPO, "tests", "golden")
 PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
 METRIC = "FOM 1/(relerr²·s) & segments/s: learned+FP32 vs plain FP64 GPU at same error"
-WORKLOAD = ("1D linearized slab, 2000 cells dx=0.005, dt=0.005 to t=3.0 (601 timesteps), NINPUT=2e6, NMAX=2e7, "
-            "sigma_a=1, c=a=1, source 1.0 on [0,0.5], FP32 particle state, FP64 material update")
-# algorithmic bytes of the 1D FP32 transport kernel: every transported
-# particle reads t, x, mu, E, E0, cell|scale (4 B each) and its alive byte;
-# every census particle writes t, x, mu, E back
+# bench decks: file, description, FP64 ensemble mean (None = no FOM)
+DECKS = {
+    "c2": ("c2_slab_fine.txt",
+           "1D linearized slab, 2000 cells dx=0.005, dt=0.005 to t=3.0 (601 timesteps), NINPUT=2e6, NMAX=2e7, "
+           "sigma_a=1, c=a=1, source 1.0 on [0,0.5], FP32 particle state, FP64 material update",
+           "c2_fp64_mean.npz"),
+    "c3": ("c3_heatwave.txt",
+           "1D nonlinear heat wave, 500 cells on [0,1], sigma_a=10*T^-3 (T>=1e-3), bee 0.1, T_init 0.01, "
+           "left surface T=1, RAMP dt0=1e-4 K=1.1 DTMAX=1e-2 to t=1, NINPUT=2e6, NMAX=2e7, FP32 state",
+           None),
+    "c4": ("c4_channel2d.txt",
+           "2D thin channel through thick walls, 140x40 cells over [0,7]x[0,2], channel sigma_a=0.2, walls 2000, "
+           "left segment y in [0,0.5] at T=0.5, dt=1e-3 to t=1, NINPUT=1e7, NMAX=5e7, FP32 state",
+           None),
+}
+DECK_KEY = "c2"
+DECK = os.path.join(GOLDEN, "decks", DECKS[DECK_KEY][0])
+REF_MEAN = os.path.join(GOLDEN, DECKS[DECK_KEY][2])
+WORKLOAD = DECKS[DECK_KEY][1]
+# algorithmic bytes of the FP32 transport kernel: every transported particle
+# reads its state (1D t, x, mu, E, E0, cell|scale; 2D adds y, uy; 4 B each)
+# and its alive byte; every census particle writes t, x, (y,) direction and E
 READ_B, WRITE_B = 25, 16
+
+
+def select_deck(key):
+    global DECK_KEY, DECK, REF_MEAN, WORKLOAD, READ_B, WRITE_B
+    DECK_KEY = key
+    DECK = os.path.join(GOLDEN, "decks", DECKS[key][0])
+    REF_MEAN = os.path.join(GOLDEN, DECKS[key][2]) if DECKS[key][2] else ""
+    WORKLOAD = DECKS[key][1]
+    READ_B, WRITE_B = (33, 24) if key == "c4" else (25, 16)
 
 for _p in (PKG, os.path.join(REPO, "oracle")):
     if _p not in sys.path:
@@ -172,12 +197,14 @@ def cpu_baseline(threads, steps=120):
     the particle counts, first `steps` timesteps; segments per second."""
     import oracle
     import mpimc
-    inputs, mesh = load_deck(0, NINPUT="20000", NMAX="200000")
+    base = mpimc.Input.readInputs(DECK)
+    n_in, n_max = int(float(base["NINPUT"])) // 100, int(float(base["NMAX"])) // 100
+    inputs, mesh = load_deck(0, NINPUT=str(n_in), NMAX=str(n_max))
     d, keep = mpimc.build_deck(inputs, mesh)
     secs, segs, hist = oracle.bench(d, threads, steps)
     return {"value": segs / secs, "unit": "segments/s", "cores": threads, "kind": "port",
-            "sample": "oracle FP32 on the same deck at NINPUT=2e4, NMAX=2e5, first %d of 601 timesteps, "
-                      "%d replicas (seeds 12345+i), %.1f s" % (steps, threads, secs),
+            "sample": "oracle FP32 on the same deck at NINPUT=%d, NMAX=%d (1/100), first %d timesteps, "
+                      "%d replicas (seeds SEED+i), %.1f s" % (n_in, n_max, steps, threads, secs),
             "histories_per_s": hist / secs}
 
 
@@ -209,6 +236,25 @@ def bench_reference(args):
     return 0
 
 
+def profile_case():
+    """The workload at half the particle counts (C2: NINPUT 1e6, NMAX 1e7, a
+    census of ~1e7 particles, ~0.25 GB of state -- larger than L2 but a few GB
+    on the device at most), stepped 12 times stage by stage; for ncu captures."""
+    import mpimc
+    from mpimc import _build
+    _build.build()
+    base = mpimc.Input.readInputs(DECK)
+    inputs, mesh = load_deck(0, NINPUT=str(int(float(base["NINPUT"]) // 2)), NMAX=str(int(float(base["NMAX"]) // 2)))
+    eng = mpimc.Engine(inputs, mesh)
+    for _ in range(12):
+        st, done = eng.step()
+        if done:
+            break
+    print(json.dumps({"profile_case": DECK_KEY, "census": st["n_census_out"], "segments": st["segments"]}))
+    eng.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -217,7 +263,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparator run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--deck", default="c2", choices=sorted(DECKS), help="workload (c2 is the headline)")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling case for ncu: the deck at half the particle counts, 12 timesteps, then exit")
     args = ap.parse_args()
+    select_deck(args.deck)
+    if args.profile:
+        return profile_case()
     rank, world, local = _env_rank()
     if world > 1:
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
@@ -271,7 +323,7 @@ def main():
     achieved = bytes_per_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": (achieved / hbm) if (achieved and hbm) else None, "traffic": None,
-                "kernel": "k_transport1d<StF32>", "avg_launch_ms": avg_ms, "launches": tr_n,
+                "kernel": "k_transport2d<StF32>" if DECK_KEY == "c4" else "k_transport1d<StF32>", "avg_launch_ms": avg_ms, "launches": tr_n,
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "transport_share_of_step": tr_ms / dev_ms if dev_ms else None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"}
@@ -279,7 +331,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (in-repo deck, seeded Philox streams)",
-        "config": {"workload": WORKLOAD, "step": "one full simulation t=0..3 (601 timesteps)",
+        "config": {"workload": WORKLOAD, "deck": DECKS[DECK_KEY][0], "step": "one full simulation",
                    "l2": "inputs larger than L2 (particle state ~0.6 GB); no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "histories_per_s": hist / (t_max / 1000.0),
