@@ -112,7 +112,7 @@ typedef struct ImcDeck {
     double temp_floor;         /* opacity temperature clamp T >= temp_floor (0 = off; not in the reference) */
     uint64_t seed;             /* SEED */
     int32_t timestepping;      /* IMC_TS_CONSTANT / IMC_TS_RAMP (TIMESTEPPING) */
-    int32_t sort_census;       /* reorder the census by cell after each step (0 = reference order) */
+    int32_t sort_census;       /* reserved, must be 0 */
     double dt, dt0, k, dtmax, t_end;  /* DT, DT0, K, DTMAX, ENDTIME */
     int64_t capacity;          /* particle-buffer capacity; 0 = derived from NMAX */
     int64_t segment_cap;       /* per-history segment cap; 0 = 1e7 */
@@ -207,7 +207,10 @@ int imc_timestep(ImcHandle *h, int *done);
 
 /* One timestep: update -> sourcing -> transport -> clean -> tally ->
  * energycheck -> timestep (src/MixedPrecisionIMC.jl:136-152).  stats may be
- * NULL.  *done = 1 once t > t_end. */
+ * NULL.  *done = 1 once t > t_end.  In imc_step and imc_run the clean stage
+ * removes killed particles only once they exceed 1/16 of the list; until then
+ * they stay in place as holes (alive byte 0; E0 = -1 in imc_get_particles)
+ * and births are appended after them.  imc_clean always removes them all. */
 int imc_step(ImcHandle *h, ImcStepStats *stats, int *done);
 /* Run steps until t > t_end or max_steps steps ran, replaying one captured
  * CUDA graph per step.  stats (may be NULL) receives up to max_steps entries;
@@ -223,7 +226,8 @@ int imc_get_time(const ImcHandle *h, double *t, double *dt, int64_t *step_index)
 /* Overrides t and dt (the reference tests build SimVars by hand,
  * test/runtests.jl:67). */
 int imc_set_time(ImcHandle *h, double t, double dt);
-/* number of particles in the list (census + any sourced, not yet cleaned) */
+/* length of the particle list: live particles, births not yet transported,
+ * and killed particles not yet removed */
 int imc_num_particles(const ImcHandle *h, int64_t *n);
 /* copy a cell field (IMC_FIELD_*) to / from the host; count = ncells, or
  * ncells*n_scales for ENERGYDEP / EMITTED. */

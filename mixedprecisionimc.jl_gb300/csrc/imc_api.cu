@@ -41,15 +41,14 @@ struct ImcHandle {
     Scalars *d_sc = nullptr;
     std::vector<void *> allocs;  // cell / scratch allocations
     // particle buffers
-    PBufRaw buf[2]{};
+    PBufRaw buf[2]{};   // which one holds the list is Scalars::cur, on the device
     std::vector<void *> pallocs;
-    int cur = 0;
     long long capacity = 0, ntiles_cap = 0;
     long long *tile_cnt = nullptr, *tile_off = nullptr;
     DevStats *d_stats = nullptr;
     long long stats_cap = 0;
     int grid_transport = 0, block_transport = 256, grid_emit = 0;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph = nullptr;  // one step, captured once
     bool timing = false;
     cudaEvent_t ev[2] = {nullptr, nullptr};
     std::vector<cudaEvent_t> ev_pool;
@@ -135,8 +134,14 @@ void free_list(std::vector<void *> &list) {
 }
 
 void drop_graphs(ImcHandle *h) {
-    for (int p = 0; p < 2; ++p)
-        if (h->graph[p]) { cudaGraphExecDestroy(h->graph[p]); h->graph[p] = nullptr; }
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+}
+
+PBufPair pair(const ImcHandle *h) {
+    PBufPair p;
+    p.b[0] = h->buf[0];
+    p.b[1] = h->buf[1];
+    return p;
 }
 
 long long births_bound(const ImcHandle *h, long long n_census) {
@@ -170,7 +175,7 @@ int grow(ImcHandle *h, long long need) {
     int rc = alloc_particles(h, ncap, nb, nlist);
     if (rc) { free_list(nlist); h->capacity = old_cap; return rc; }
     const size_t se = state_elem(h->prec), e0 = e0_elem(h->prec);
-    const PBufRaw &o = h->buf[h->cur];
+    const PBufRaw &o = h->buf[sc.cur];
     PBufRaw &w = nb[0];
     if (n > 0) {
         CK(h, cudaMemcpy(w.t, o.t, se * n, cudaMemcpyDeviceToDevice));
@@ -189,7 +194,8 @@ int grow(ImcHandle *h, long long need) {
     h->pallocs = nlist;
     h->buf[0] = nb[0];
     h->buf[1] = nb[1];
-    h->cur = 0;
+    sc.cur = 0;
+    CK(h, cudaMemcpy(h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice));
     h->ca.capacity = ncap;
     if ((rc = tile_alloc(h))) return rc;
     drop_graphs(h);
@@ -246,17 +252,18 @@ void host_timestep(const ImcDeck &d, double &t, double &dt, bool &finished) {
     finished = t > d.t_end;
 }
 
-// the kernel sequence of one step, asynchronous on h->stream
-int enqueue_step(ImcHandle *h, int parity, bool with_events, int ev_slot) {
-    PBufRaw src = h->buf[parity], dst = h->buf[parity ^ 1];
+// the kernel sequence of one step, asynchronous on h->stream; the list's
+// buffer is chosen on the device, so the same sequence serves every step
+int enqueue_step(ImcHandle *h, bool with_events, int ev_slot) {
+    const PBufPair bufs = pair(h);
     cudaStream_t st = h->stream;
     launch_update(h->ca, h->d_sc, st);
-    launch_source(h->ca, h->d_sc, h->prec, src, h->grid_emit, st);
+    launch_source(h->ca, h->d_sc, h->prec, bufs, h->grid_emit, st);
     if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot], st));
-    launch_transport(h->ca, h->d_sc, h->prec, src, h->grid_transport, st);
+    launch_transport(h->ca, h->d_sc, h->prec, bufs, h->grid_transport, st);
     if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot + 1], st));
     launch_finalize(h->ca, h->d_sc, st);
-    launch_compact(h->ca, h->d_sc, h->prec, src, dst, h->tile_cnt, h->tile_off, h->ntiles_cap, st);
+    launch_compact(h->ca, h->d_sc, h->prec, bufs, h->tile_cnt, h->tile_off, h->ntiles_cap, false, st);
     launch_tally(h->ca, h->d_sc, st);
     launch_energycheck(h->ca, h->d_sc, h->d_stats, h->stats_cap, st);
     launch_timestep(h->ca, h->d_sc, st);
@@ -295,15 +302,15 @@ int ensure_stats(ImcHandle *h, long long n) {
     return IMC_OK;
 }
 
-int capture(ImcHandle *h, int parity) {
-    if (h->graph[parity]) return IMC_OK;
+int capture(ImcHandle *h) {
+    if (h->graph) return IMC_OK;
     cudaGraph_t g;
     CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_step(h, parity, false, 0);
+    int rc = enqueue_step(h, false, 0);
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
     if (rc) return rc;
     if (e != cudaSuccess) return fail(h, IMC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&h->graph[parity], g, 0);
+    e = cudaGraphInstantiate(&h->graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(h, IMC_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     return IMC_OK;
@@ -521,7 +528,7 @@ int imc_sourcing(ImcHandle *h) {
     int rc = read_scalars(h, &sc);
     if (rc) return rc;
     if ((rc = grow(h, sc.n_particles + births_bound(h, sc.n_particles)))) return rc;
-    launch_source(h->ca, h->d_sc, h->prec, h->buf[h->cur], h->grid_emit, h->stream);
+    launch_source(h->ca, h->d_sc, h->prec, pair(h), h->grid_emit, h->stream);
     CKL(h);
     if ((rc = read_scalars(h, &sc))) return rc;
     h->stage = Stage::Sourced;
@@ -533,7 +540,7 @@ int imc_transport(ImcHandle *h) {
     if (!h) return IMC_ERR_INVALID_ARG;
     if (h->stage != Stage::Sourced) launch_prepare_transport(h->ca, h->d_sc, h->stream);
     if (h->timing) CK(h, cudaEventRecord(h->ev[0], h->stream));
-    launch_transport(h->ca, h->d_sc, h->prec, h->buf[h->cur], h->grid_transport, h->stream);
+    launch_transport(h->ca, h->d_sc, h->prec, pair(h), h->grid_transport, h->stream);
     CKL(h);
     if (h->timing) {
         CK(h, cudaEventRecord(h->ev[1], h->stream));
@@ -554,11 +561,10 @@ int imc_transport(ImcHandle *h) {
 
 int imc_clean(ImcHandle *h) {
     if (!h) return IMC_ERR_INVALID_ARG;
-    launch_compact(h->ca, h->d_sc, h->prec, h->buf[h->cur], h->buf[h->cur ^ 1], h->tile_cnt, h->tile_off,
-                   h->ntiles_cap, h->stream);
+    // Clean.clean removes every killed particle (forced compaction)
+    launch_compact(h->ca, h->d_sc, h->prec, pair(h), h->tile_cnt, h->tile_off, h->ntiles_cap, true, h->stream);
     CKL(h);
     CK(h, cudaStreamSynchronize(h->stream));
-    h->cur ^= 1;
     h->stage = Stage::Cleaned;
     return IMC_OK;
 }
@@ -611,14 +617,13 @@ int imc_step(ImcHandle *h, ImcStepStats *stats, int *done) {
     if ((rc = grow(h, sc.n_particles + births_bound(h, sc.n_particles)))) return rc;
     if (h->timing) {
         if ((rc = ensure_events(h, 1))) return rc;
-        if ((rc = enqueue_step(h, h->cur, true, 0))) return rc;
+        if ((rc = enqueue_step(h, true, 0))) return rc;
     } else {
-        if ((rc = capture(h, h->cur))) return rc;
-        CK(h, cudaGraphLaunch(h->graph[h->cur], h->stream));
+        if ((rc = capture(h))) return rc;
+        CK(h, cudaGraphLaunch(h->graph, h->stream));
     }
     if ((rc = read_scalars(h, &sc))) return rc;
     if (h->timing && (rc = collect_events(h, 1))) return rc;
-    h->cur ^= 1;
     DevStats ds;
     CK(h, cudaMemcpy(&ds, h->d_stats + ((sc.step - 1u) % (unsigned long long)h->stats_cap), sizeof(DevStats),
                      cudaMemcpyDeviceToHost));
@@ -675,16 +680,11 @@ int imc_run(ImcHandle *h, int64_t max_steps, ImcStepStats *stats, int64_t *n_ste
         }
         if (h->timing) {
             if ((rc = ensure_events(h, (size_t)m))) return rc;
-            for (int64_t s = 0; s < m; ++s) {
-                if ((rc = enqueue_step(h, h->cur, true, (int)s))) return rc;
-                h->cur ^= 1;
-            }
+            for (int64_t s = 0; s < m; ++s)
+                if ((rc = enqueue_step(h, true, (int)s))) return rc;
         } else {
-            for (int64_t s = 0; s < m; ++s) {
-                if ((rc = capture(h, h->cur))) return rc;
-                CK(h, cudaGraphLaunch(h->graph[h->cur], h->stream));
-                h->cur ^= 1;
-            }
+            if ((rc = capture(h))) return rc;
+            for (int64_t s = 0; s < m; ++s) CK(h, cudaGraphLaunch(h->graph, h->stream));
         }
         done_steps += m;
         if ((rc = read_scalars(h, &sc))) return rc;
@@ -797,7 +797,7 @@ int imc_get_particles(const ImcHandle *hc, ImcParticles *p) {
     if (rc) return rc;
     const long long n = sc.n_particles;
     if (n > p->n) return fail(h, IMC_ERR_INVALID_ARG, "particle arrays too small");
-    const PBufRaw &b = h->buf[h->cur];
+    const PBufRaw &b = h->buf[sc.cur];
     const size_t se = state_elem(h->prec), e0 = e0_elem(h->prec);
     std::vector<unsigned char> t(se * n), x(se * n), y(se * n), ux(se * n), uy(se * n), E(se * n), E0(e0 * n);
     std::vector<int32_t> cs(n);
@@ -899,7 +899,9 @@ int imc_set_particles(ImcHandle *h, const ImcParticles *p) {
         wr(ux, i, dirx);
         wr(uy, i, diry);
     }
-    const PBufRaw &b = h->buf[h->cur];
+    Scalars sc;
+    if ((rc = read_scalars(h, &sc))) return rc;
+    const PBufRaw &b = h->buf[sc.cur];
     if (n > 0) {
         CK(h, cudaMemcpy(b.t, t.data(), se * n, cudaMemcpyHostToDevice));
         CK(h, cudaMemcpy(b.x, x.data(), se * n, cudaMemcpyHostToDevice));
@@ -913,9 +915,9 @@ int imc_set_particles(ImcHandle *h, const ImcParticles *p) {
         CK(h, cudaMemcpy(b.cs, cs.data(), 4 * n, cudaMemcpyHostToDevice));
         CK(h, cudaMemcpy(b.alive, alive.data(), n, cudaMemcpyHostToDevice));
     }
-    Scalars sc;
-    if ((rc = read_scalars(h, &sc))) return rc;
-    sc.n_census = n;
+    long long live = 0;
+    for (long long i = 0; i < n; ++i) live += alive[i];
+    sc.n_census = live;
     sc.n_particles = n;
     union { double d; unsigned long long u; } cv;
     cv.d = emax;

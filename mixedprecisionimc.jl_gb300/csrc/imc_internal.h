@@ -29,9 +29,10 @@ struct Scalars {
     double lost_step;                  // escaped energy of this step
     unsigned long long emax_census_bits;  // max census energy (bits of a non-negative double)
     double emax;                       // max particle energy at transport start
-    long long n_census;                // census (after clean); start of the list
+    long long n_census;                // live particles in the list (the census after transport)
     long long n_census_in;             // census carried into this step
-    long long n_particles;             // list length after sourcing
+    long long n_particles;             // list length (live particles and holes left by kills)
+    long long birth_base;              // list index of this step's first birth
     long long n_sourced;
     double n_source;                   // particle budget of this step
     unsigned long long segments;
@@ -40,7 +41,9 @@ struct Scalars {
     int b_dep, b_rad, b_lost;          // fixed-point exponents of this transport
     unsigned int step;                 // step index (RNG key, stats slot)
     int finished;                      // t > t_end
-    int pad;
+    int cur;                           // particle buffer holding the list (0 or 1)
+    int compact_src;                   // buffer compacted from this step
+    int compact_now;                   // this step compacts the list
 };
 
 struct CellArgs {
@@ -77,6 +80,12 @@ struct PBufRaw {
     uint8_t *alive;
 };
 
+// the two particle buffers; Scalars::cur says which one holds the list, so
+// the kernels of a step need no host-side knowledge of it
+struct PBufPair {
+    PBufRaw b[2];
+};
+
 // per-step statistics slot written on the device
 struct DevStats {
     double t, dt, total_energy, energy_dep, rad_energy, rad_energy_old, lost_energy, energy_error;
@@ -86,14 +95,21 @@ struct DevStats {
 
 // launchers (imc_kernels.cu / imc_transport.cu); all asynchronous on `st`
 void launch_update(const CellArgs &ca, Scalars *sc, cudaStream_t st);
-void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, cudaStream_t st);
+void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, int grid, cudaStream_t st);
 struct TransportShape {
     bool smem_tally;  // block-private tallies in shared memory
     int smem;         // dynamic shared memory bytes
     int block;        // threads per block
 };
 TransportShape transport_shape(const CellArgs &ca, int prec);
-void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, cudaStream_t st);
+void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, int grid, cudaStream_t st);
+// Removes killed particles from the list.  With force = false the list is
+// compacted only when the holes exceed 1/16 of its length (kDeferHoles);
+// otherwise the holes stay and only the live count is updated.
+constexpr long long kDeferHoles = 16;
+void launch_compact(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, long long *tile_cnt,
+                    long long *tile_off, long long ntiles_cap, bool force, cudaStream_t st);
+// forced compaction of `src` into `dst` (the list must be in src: Scalars::cur == 0)
 void launch_compact(const CellArgs &ca, Scalars *sc, int prec, PBufRaw src, PBufRaw dst, long long *tile_cnt,
                     long long *tile_off, long long ntiles_cap, cudaStream_t st);
 void launch_finalize(const CellArgs &ca, Scalars *sc, cudaStream_t st);

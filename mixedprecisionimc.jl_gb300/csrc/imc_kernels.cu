@@ -326,11 +326,12 @@ __global__ void __launch_bounds__(kPlanThreads) k_source_scan(CellArgs ca, Scala
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        const long long n_census = sc->n_census;
+        const long long n_census = sc->n_census;  // live particles
+        const long long len = sc->n_particles;    // list length, holes included
         long long n_new = s_run;
         unsigned fl = 0;
-        if (n_census + n_new > ca.capacity) {
-            n_new = ca.capacity - n_census;
+        if (len + n_new > ca.capacity) {
+            n_new = ca.capacity - len;
             if (n_new < 0) n_new = 0;
             fl |= 1u << 3;
         }
@@ -338,7 +339,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_source_scan(CellArgs ca, Scala
         for (int bb = 0; bb < ca.nblk_slot; ++bb) emax = fmax(emax, ca.part_emax[bb]);
         sc->n_census_in = n_census;
         sc->n_sourced = n_new;
-        sc->n_particles = n_census + n_new;
+        sc->birth_base = len;
+        sc->n_particles = len + n_new;
         sc->emax = emax;
         sc->emax_census_bits = 0ull;
         sc->segments = 0ull;
@@ -387,10 +389,10 @@ __device__ __forceinline__ void store_birth(const CellArgs &ca, PBuf<St> &pb, lo
 
 // One thread per newborn particle; its stream is keyed by its list index.
 template <class St>
-__global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, PBufRaw raw) {
+__global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, PBufPair bufs) {
     typedef typename St::T T;
-    PBuf<St> pb(raw);
-    const long long n_new = sc->n_sourced, n_census = sc->n_census_in;
+    PBuf<St> pb(bufs.b[sc->cur]);
+    const long long n_new = sc->n_sourced, n_census = sc->birth_base;
     const unsigned step = sc->step;
     const double dtd = sc->dt;
     const T dtT = (T)dtd, dsT = (T)ca.ds;
@@ -484,7 +486,7 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
     }
 }
 
-void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, cudaStream_t st) {
+void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufPair buf, int grid, cudaStream_t st) {
     const int nb = ca.nblk_slot;
     k_source_slots<<<nb, kCellThreads, 0, st>>>(ca, sc);
     k_source_total<<<1, 192, 0, st>>>(ca, sc);
@@ -499,8 +501,9 @@ void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int g
 // Stable three-pass compaction: per-tile alive counts, one-block exclusive
 // scan of the tile counts, then a per-tile block scan that scatters the
 // survivors in order into the other buffer.
-__global__ void __launch_bounds__(kCompactThreads) k_compact_count(const Scalars *sc, const uint8_t *alive,
+__global__ void __launch_bounds__(kCompactThreads) k_compact_count(const Scalars *sc, PBufPair bufs,
                                                                    long long *tile_cnt) {
+    const uint8_t *alive = bufs.b[sc->cur].alive;
     const long long n = sc->n_particles;
     const long long base = (long long)blockIdx.x * kCompactTile;
     if (base >= n) return;
@@ -520,7 +523,8 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_count(const Scalars
     }
 }
 
-__global__ void __launch_bounds__(1024) k_compact_scan(Scalars *sc, const long long *tile_cnt, long long *tile_off) {
+__global__ void __launch_bounds__(1024) k_compact_scan(Scalars *sc, const long long *tile_cnt, long long *tile_off,
+                                                      int force) {
     __shared__ long long warp_tot[32];
     __shared__ long long s_run;
     const long long n = sc->n_particles;
@@ -554,8 +558,16 @@ __global__ void __launch_bounds__(1024) k_compact_scan(Scalars *sc, const long l
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        sc->n_census = s_run;
-        sc->n_particles = s_run;
+        // compact when forced (Clean.clean) or when the holes exceed 1/16 of the list
+        const long long alive = s_run;
+        const bool compact = force || (n - alive) * kDeferHoles > n;
+        sc->n_census = alive;
+        sc->compact_now = compact ? 1 : 0;
+        if (compact) {
+            sc->compact_src = sc->cur;
+            sc->cur ^= 1;
+            sc->n_particles = alive;
+        }
     }
 }
 
@@ -574,9 +586,10 @@ __device__ __forceinline__ void scatter_field(const V *src, V *dst, long long ba
 
 template <class St>
 __global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(int geometry, const Scalars *sc,
-                                                                     const long long *tile_off, PBufRaw sraw,
-                                                                     PBufRaw draw, const long long *n_before) {
-    PBuf<St> src(sraw), dst(draw);
+                                                                     const long long *tile_off, PBufPair bufs,
+                                                                     const long long *n_before) {
+    if (!sc->compact_now) return;
+    PBuf<St> src(bufs.b[sc->compact_src]), dst(bufs.b[sc->compact_src ^ 1]);
     __shared__ unsigned short src_idx[kCompactTile];
     __shared__ __align__(16) unsigned char stage[kCompactTile * 8];
     __shared__ int wt[kCompactThreads / 32];
@@ -586,25 +599,40 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(int geometr
     if (base >= n) return;
     const int tile_n = (int)((n - base) < kCompactTile ? (n - base) : kCompactTile);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // survivor list of the tile, in order
-    int run = 0;
-    for (int r = 0; r < kCompactTile; r += kCompactThreads) {
-        const int i = r + threadIdx.x;
-        const bool f = i < tile_n && src.alive[base + i];
-        const unsigned m = __ballot_sync(0xFFFFFFFFu, f);
-        const int wpre = __popc(m & ((1u << lane) - 1u));
-        if (lane == 0) wt[warp] = __popc(m);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int acc = 0;
-            for (int w = 0; w < kCompactThreads / 32; ++w) { int v = wt[w]; wt[w] = acc; acc += v; }
-            s_tot = acc;
-        }
-        __syncthreads();
-        if (f) src_idx[run + wt[warp] + wpre] = (unsigned short)i;
-        run += s_tot;
-        __syncthreads();
+    // survivor list of the tile, in order: thread t owns tile positions
+    // [16t, 16t + 16) and reads their alive bytes with one 16-byte load
+    constexpr int kPer = kCompactTile / kCompactThreads;
+    static_assert(kPer == 16, "one uint4 of alive bytes per thread");
+    const int first = threadIdx.x * kPer;
+    unsigned char flags[kPer];
+    const uint8_t *ap = src.alive + base + first;
+    if (first + kPer <= tile_n && (((uintptr_t)ap) & 15u) == 0) {
+        uint4 v = *reinterpret_cast<const uint4 *>(ap);
+        const unsigned w[4] = {v.x, v.y, v.z, v.w};
+        for (int q = 0; q < kPer; ++q) flags[q] = (unsigned char)((w[q >> 2] >> (8 * (q & 3))) & 0xFFu);
+    } else {
+        for (int q = 0; q < kPer; ++q) flags[q] = first + q < tile_n ? ap[q] : 0;
     }
+    int mine = 0;
+    for (int q = 0; q < kPer; ++q) mine += flags[q] ? 1 : 0;
+    int incl = mine;
+    for (int off = 1; off < 32; off <<= 1) {
+        int y = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+        if (lane >= off) incl += y;
+    }
+    if (lane == 31) wt[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int w = 0; w < kCompactThreads / 32; ++w) { int v = wt[w]; wt[w] = acc; acc += v; }
+        s_tot = acc;
+    }
+    __syncthreads();
+    int pos = wt[warp] + incl - mine;
+    for (int q = 0; q < kPer; ++q)
+        if (flags[q]) src_idx[pos++] = (unsigned short)(first + q);
+    const int run = s_tot;
+    __syncthreads();
     const int cnt = run;
     const long long out = tile_off[blockIdx.x];
     scatter_field(src.t, dst.t, base, tile_n, out, cnt, src_idx, stage);
@@ -622,19 +650,27 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(int geometr
 
 __global__ void k_copy_count(const Scalars *sc, long long *n_before) { *n_before = sc->n_particles; }
 
-void launch_compact(const CellArgs &ca, Scalars *sc, int prec, PBufRaw src, PBufRaw dst, long long *tile_cnt,
-                    long long *tile_off, long long ntiles_cap, cudaStream_t st) {
+void launch_compact(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, long long *tile_cnt,
+                    long long *tile_off, long long ntiles_cap, bool force, cudaStream_t st) {
     // tile_off has ntiles_cap + 1 entries; the last holds the pre-compaction length
     long long *n_before = tile_off + ntiles_cap;
     k_copy_count<<<1, 1, 0, st>>>(sc, n_before);
-    k_compact_count<<<(unsigned)ntiles_cap, kCompactThreads, 0, st>>>(sc, src.alive, tile_cnt);
-    k_compact_scan<<<1, 1024, 0, st>>>(sc, tile_cnt, tile_off);
+    k_compact_count<<<(unsigned)ntiles_cap, kCompactThreads, 0, st>>>(sc, bufs, tile_cnt);
+    k_compact_scan<<<1, 1024, 0, st>>>(sc, tile_cnt, tile_off, force ? 1 : 0);
     if (prec == 0)
-        k_compact_scatter<StF64><<<(unsigned)ntiles_cap, kCompactThreads, 0, st>>>(ca.geometry, sc, tile_off, src, dst, n_before);
+        k_compact_scatter<StF64><<<(unsigned)ntiles_cap, kCompactThreads, 0, st>>>(ca.geometry, sc, tile_off, bufs, n_before);
     else if (prec == 1)
-        k_compact_scatter<StF32><<<(unsigned)ntiles_cap, kCompactThreads, 0, st>>>(ca.geometry, sc, tile_off, src, dst, n_before);
+        k_compact_scatter<StF32><<<(unsigned)ntiles_cap, kCompactThreads, 0, st>>>(ca.geometry, sc, tile_off, bufs, n_before);
     else
-        k_compact_scatter<StF16><<<(unsigned)ntiles_cap, kCompactThreads, 0, st>>>(ca.geometry, sc, tile_off, src, dst, n_before);
+        k_compact_scatter<StF16><<<(unsigned)ntiles_cap, kCompactThreads, 0, st>>>(ca.geometry, sc, tile_off, bufs, n_before);
+}
+
+void launch_compact(const CellArgs &ca, Scalars *sc, int prec, PBufRaw src, PBufRaw dst, long long *tile_cnt,
+                    long long *tile_off, long long ntiles_cap, cudaStream_t st) {
+    PBufPair p;
+    p.b[0] = src;
+    p.b[1] = dst;
+    launch_compact(ca, sc, prec, p, tile_cnt, tile_off, ntiles_cap, true, st);
 }
 
 // ------------------------------------------------------------------- tally
@@ -805,7 +841,7 @@ __global__ void k_prepare_transport(CellArgs ca, Scalars *sc) {
     sc->surrogate_calls = 0ull;
     sc->n_census_in = sc->n_census;
     sc->n_sourced = 0;
-    sc->n_particles = sc->n_census;
+    sc->birth_base = sc->n_particles;
     sc->b_dep = fix_exponent(emax / ca.vol_min);
     sc->b_lost = fix_exponent(emax);
     sc->b_rad = fix_exponent(emax);

@@ -128,9 +128,9 @@ __device__ __forceinline__ void finish_counters(Scalars *sc, unsigned long long 
 }
 
 template <class St, int BLOCK, bool SMT>
-__global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc, PBufRaw raw) {
+__global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc, PBufPair bufs) {
     typedef typename St::T T;
-    PBuf<St> pb(raw);
+    PBuf<St> pb(bufs.b[sc->cur]);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Tab1<T> *tab = reinterpret_cast<Tab1<T> *>(smem_raw);
     const int N = ca.nx;
@@ -275,9 +275,9 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
 }
 
 template <class St, int BLOCK, bool SMT>
-__global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc, PBufRaw raw) {
+__global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc, PBufPair bufs) {
     typedef typename St::T T;
-    PBuf<St> pb(raw);
+    PBuf<St> pb(bufs.b[sc->cur]);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int NX = ca.nx, NY = ca.ny, nc = ca.nc;
     Tab2<T> *tab = reinterpret_cast<Tab2<T> *>(smem_raw);
@@ -481,12 +481,12 @@ const void *transport_kernel_ptr(const CellArgs &ca, int prec) {
 }
 
 template <class St, int B, bool SMT>
-static void launch_one(const CellArgs &ca, Scalars *sc, PBufRaw buf, int grid, int smem, cudaStream_t st) {
+static void launch_one(const CellArgs &ca, Scalars *sc, PBufPair buf, int grid, int smem, cudaStream_t st) {
     if (ca.geometry == 1) k_transport1d<St, B, SMT><<<grid, B, smem, st>>>(ca, sc, buf);
     else k_transport2d<St, B, SMT><<<grid, B, smem, st>>>(ca, sc, buf);
 }
 
-void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufRaw buf, int grid, cudaStream_t st) {
+void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufPair buf, int grid, cudaStream_t st) {
     TransportShape sh = transport_shape(ca, prec);
     if (sh.smem_tally) {
         if (prec == 0) launch_one<StF64, 512, true>(ca, sc, buf, grid, sh.smem, st);

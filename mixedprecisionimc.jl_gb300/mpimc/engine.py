@@ -90,7 +90,7 @@ def build_deck(inputs, mesh, overrides=None):
     d.seed = int(inputs.get("SEED", "0")) & ((1 << 64) - 1)
     ts = str(inputs.get("TIMESTEPPING", "CONSTANT")).strip().upper()
     d.timestepping = _lib.IMC_TS_RAMP if ts == "RAMP" else _lib.IMC_TS_CONSTANT
-    d.sort_census = 1 if _flag(inputs, "SORTCENSUS") else 0
+    d.sort_census = 0
     # the clock is FP64 for every PRECISION (timestep control stays on the
     # host in FP64), so DT / ENDTIME are not rounded to the deck precision
     f64 = lambda k: float(inputs[k])

@@ -308,8 +308,10 @@ void orc_sourcing_impl(Sim &s) {
     s.totalenergy = sum_body.val() + sum_rad.val() + e_surface;
     const double E = s.totalenergy;
 
-    /* particle budget (src/imc_sourcing.jl:132-136); length(Ncells) is 1 in 1D, 2 in 2D */
-    int64_t n_census = (int64_t)s.parts.size();
+    /* particle budget (src/imc_sourcing.jl:132-136) on the live census;
+     * length(Ncells) is 1 in 1D, 2 in 2D */
+    int64_t n_census = 0;
+    for (const OP &q : s.parts) n_census += q.alive ? 1 : 0;
     double n_source = (double)s.d.n_input;
     if (s.d.n_input + n_census > s.d.n_max) {
         double lenN = s.d.geometry == IMC_GEOM_1D ? 1.0 : 2.0;
@@ -352,7 +354,7 @@ void orc_sourcing_impl(Sim &s) {
     for (auto &sl : slots) total += sl.count;
     s.n_sourced = total;
     const T dtT = (T)dt, dsT = (T)ds;
-    int64_t pid = n_census;
+    int64_t pid = (int64_t)s.parts.size();  /* births follow the list, holes included */
     s.parts.reserve(s.parts.size() + total);
     for (auto &sl : slots) {
         for (int64_t q = 0; q < sl.count; ++q, ++pid) {
@@ -683,9 +685,22 @@ void orc_clean_impl(Sim &s) {
     for (size_t r = 0; r < s.parts.size(); ++r)
         if (s.parts[r].alive) s.parts[w++] = s.parts[r];
     s.parts.resize(w);
-    if (s.d.sort_census) {
-        std::stable_sort(s.parts.begin(), s.parts.end(), [](const OP &a, const OP &b) { return a.cell < b.cell; });
-    }
+}
+
+/* The engine's whole-step list policy: killed particles stay in the list as
+ * holes until they exceed 1/16 of its length, then the list is compacted as
+ * Clean.clean does.  Births are appended after the holes, so a history's list
+ * index -- the key of its random stream -- is the same here and on the GPU. */
+void step_clean(Sim &s) {
+    int64_t len = (int64_t)s.parts.size(), live = 0;
+    for (const OP &q : s.parts) live += q.alive ? 1 : 0;
+    if ((len - live) * 16 > len) orc_clean_impl(s);
+}
+
+int64_t live_count(const Sim &s) {
+    int64_t n = 0;
+    for (const OP &q : s.parts) n += q.alive ? 1 : 0;
+    return n;
 }
 
 /* physical energy of a stored particle */
@@ -829,7 +844,7 @@ void fill_stats(Sim &s, ImcStepStats *st, double t, double dt) {
     st->energy_error = s.last_err;
     st->n_census_in = s.n_census_in;
     st->n_sourced = s.n_sourced;
-    st->n_census_out = (int64_t)s.parts.size();
+    st->n_census_out = live_count(s);
     st->segments = s.segments;
     st->surrogate_calls = 0;
     st->error_flags = s.flags;
@@ -842,7 +857,7 @@ int step_impl(Sim &s, ImcStepStats *st, int *done) {
     orc_update_impl(s);
     orc_sourcing_dispatch(s);
     orc_transport_impl(s);
-    orc_clean_impl(s);
+    step_clean(s);
     orc_tally_impl(s);
     orc_energycheck_impl(s);
     fill_stats(s, &s.last, t0, dt0);
