@@ -12,7 +12,8 @@ One bench step is one full simulation (t = 0 -> 3).  Printed on one JSON line:
                of the final cell temperature against the FP64 ensemble mean
                (tests/golden/c2_fp64_mean.npz), s = seconds per simulation
   fp64         the same deck with FP64 particle state (the plain FP64 GPU
-               path), its segments/s, relerr and FOM
+               path), as many runs as the timed steps: segments/s, relerr, FOM
+  fp16_state   one run with binary16 particle state
   e2e          segments/s through the public API with host buffers: deck
                upload, run and the read-back of the cell fields per step
   roofline     the transport kernel: algorithmic bytes per launch over its
@@ -263,6 +264,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparator run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-fp16", action="store_true", help="skip the FP16-state run")
     ap.add_argument("--deck", default="c2", choices=sorted(DECKS), help="workload (c2 is the headline)")
     ap.add_argument("--profile", action="store_true",
                     help="profiling case for ncu: the deck at half the particle counts, 12 timesteps, then exit")
@@ -343,15 +345,27 @@ def main():
         "roofline": roofline,
         "wall_s_timed": wall,
     }
+    def comparator(prec_code, seed_base, n):
+        """n full runs with another particle-state precision: speed, error, FOM"""
+        rs = [run_once(*load_deck(seed_base + 1000 * i), overrides={"precision": prec_code,
+                                                                    "scale_select_precision": prec_code})
+              for i in range(n)]
+        secs = sum(r["ms"] for r in rs) / 1000.0
+        rels = [relerr(r["temp"], ref) for r in rs]
+        rel_c = None if rels[0] is None else float(np.sqrt(np.mean(np.square(rels))))
+        fom_c = None if rel_c is None else 1.0 / (rel_c ** 2 * secs / n)
+        return {"value": sum(r["segments"] for r in rs) / secs, "unit": "segments/s", "runs": n,
+                "ms_per_step": 1000.0 * secs / n, "relerr_T": rel_c, "fom": fom_c,
+                "energy_error_max": max(r["energy_error"] for r in rs)}
+
     if not args.no_fp64:
-        r64 = run_once(*load_deck(7), overrides={"precision": 0, "scale_select_precision": 0}, timing=False)
-        s64 = r64["ms"] / 1000.0
-        rel64 = relerr(r64["temp"], ref)
-        fom64 = None if rel64 is None else 1.0 / (rel64 ** 2 * s64)
-        out["fp64"] = {"value": r64["segments"] / s64, "unit": "segments/s", "ms_per_step": r64["ms"],
-                       "relerr_T": rel64, "fom": fom64, "energy_error_max": r64["energy_error"]}
-        if fom and fom64:
-            out["fom_ratio_fp32_over_fp64"] = fom / fom64
+        # the plain FP64 GPU path, as many runs as the timed FP32 runs
+        out["fp64"] = comparator(0, 7, args.steps)
+        if fom and out["fp64"]["fom"]:
+            out["fom_ratio_fp32_over_fp64"] = fom / out["fp64"]["fom"]
+        out["time_ratio_fp64_over_fp32"] = out["fp64"]["ms_per_step"] / (dev_ms / args.steps)
+    if not args.no_fp16:
+        out["fp16_state"] = comparator(2, 11, 1)
     w, s, h2d, d2h = e2e_once(2000)
     out["e2e"] = {"value": s / w, "unit": "segments/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                   "wall_s_per_step": w}

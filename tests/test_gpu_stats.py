@@ -46,3 +46,23 @@ def test_c1_ensemble_within_3_sigma(prec, gpu_lib):
         # 100 cells: allow the odd 3-sigma excursion, bound the chi-square
         assert np.mean(np.abs(z) < 3.0) >= 0.97, (name, np.sort(np.abs(z))[-5:])
         assert np.mean(z ** 2) < 1.0 + 6.0 * np.sqrt(2.0 / live.sum()), (name, np.mean(z ** 2))
+
+
+def test_c2_fp32_ensemble_mean_matches_fp64_mean(gpu_lib):
+    """At the full 2000-cell slab size (2e7 particles, 602 steps): the mean
+    final temperature of 8 FP32-state runs agrees with the 32-seed FP64 mean
+    (tests/golden/c2_fp64_mean.npz) within 3 sigma per cell, so FP32 state
+    adds no bias to the FOM comparison."""
+    import mpimc
+    g = np.load(os.path.join(REPO, "tests", "golden", "c2_fp64_mean.npz"))
+    T = []
+    for i in range(8):
+        inputs, mesh = load_deck("c2_slab_fine", SEED=str(770000 + i))
+        e = mpimc.Engine(inputs, mesh)
+        e.run()
+        T.append(e.field("temp"))
+        e.close()
+    T = np.array(T)
+    z = (T.mean(0) - g["temp"]) / np.sqrt(T.std(0, ddof=1) ** 2 / len(T) + g["temp_std"] ** 2 / len(g["seeds"]))
+    assert np.mean(np.abs(z) < 3.0) >= 0.98, np.sort(np.abs(z))[-10:]
+    assert np.mean(z ** 2) < 1.3, np.mean(z ** 2)
