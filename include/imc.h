@@ -282,6 +282,65 @@ typedef struct ImcDeviceParticles {
 int imc_clean_noalloc(int precision, int geometry, const ImcDeviceParticles *src, ImcDeviceParticles *dst,
                       int64_t n, int64_t *n_out, void *stream);
 
+/* ---- learned thick-cell surrogate --------------------------------------- */
+
+/* Replaces the analog collision loop of Transport.MC (src/imc_transport.jl:
+ * 72-193) inside cells many mean free paths thick.  Inside one cell a history
+ * is a random walk whose outcome depends only on its state in mean free
+ * paths: distance to the nearer face d_n, to the farther face d_f, direction
+ * cosine mu' (> 0 away from the nearer face) and lmax, the path after which
+ * the walk is cut (census, or the 1 % energy cut-off).  A 4-64-64-64-64
+ * ReLU network (IMC_SURROGATE_PARAMS floats, W[out][in] row-major then the
+ * bias, per layer) maps (min(d_n/lmax,1), min(d_f/lmax,1), mu',
+ * (log10 lmax - 2)/2) to the probabilities of exit near / exit far /
+ * truncation and the quantiles of the exit path ln(l/lmax) and exit |mu|, or
+ * of the displacement/lmax toward the far face and final mu' at truncation.
+ * The transport kernel evaluates it with BF16 tensor-core MMA and FP32
+ * accumulation on batches of 16 histories per warp. */
+#define IMC_SURROGATE_PARAMS 12800
+
+typedef struct ImcSurrogateTrainConfig {
+    uint64_t seed;       /* training walks and initial weights */
+    int64_t n_samples;   /* analog in-cell walks generated on the device */
+    int32_t batch;       /* walks per Adam step; a multiple of 64 dividing n_samples */
+    int32_t iterations;  /* Adam steps */
+    float lr;            /* peak learning rate (cosine decay) */
+    float lr_min;        /* final learning rate */
+} ImcSurrogateTrainConfig;
+
+/* *count = IMC_SURROGATE_PARAMS. */
+int imc_surrogate_param_count(int *count);
+/* Generates walks and trains the network on the GPU (FP32 forward and
+ * backward, Adam).  params: IMC_SURROGATE_PARAMS floats out; loss_history:
+ * `iterations` mean batch losses out, or NULL.  Deterministic in the config. */
+int imc_surrogate_train(const ImcSurrogateTrainConfig *cfg, float *params, float *loss_history);
+/* Analog in-cell walks (the training targets) on the GPU.  state: n x 4
+ * (d_n, d_f, mu', lmax) in host memory, or NULL to draw training states.
+ * Out (host): x n x 4 network inputs, cls n outcomes (0 near, 1 far,
+ * 2 truncated), tgt n x 2 (ln(l/lmax), |mu|) or (displacement/lmax, mu'). */
+int imc_surrogate_walk(uint64_t seed, const float *state, int64_t n, float *x, int32_t *cls, float *tgt);
+/* Training loss (mean over the n samples) and its gradient with respect to
+ * the parameters, on the GPU in FP32; all buffers in host memory. */
+int imc_surrogate_grad(const float *params, const float *x, const int32_t *cls, const float *tgt, int64_t n,
+                       float *grad, double *loss);
+/* Network outputs (n x 64, host) for n inputs (n x 4, host) by the transport
+ * kernel's BF16 tensor-core forward pass. */
+int imc_surrogate_forward(const float *params, const float *x, int64_t n, float *out);
+/* Outcomes sampled from the network at n walk states (n x 4, host) as the
+ * transport kernel samples them: cls, y0, y1 as imc_surrogate_walk's. */
+int imc_surrogate_sample(const float *params, uint64_t seed, const float *state, int64_t n, int32_t *cls,
+                         float *y0, float *y1);
+/* Turns the surrogate on for this handle's transport (params: n_params ==
+ * IMC_SURROGATE_PARAMS floats, host) or off (params NULL).  1D geometry with
+ * FP32 or FP16 particle state only.  In a cell at least 8 mean free paths
+ * wide, a history with at least 32 mean free paths of path left before census
+ * or the cut-off is moved by one network query instead of its analog
+ * collisions (lmax above 1e4 is walked in 1e4 pieces); elsewhere transport
+ * is analog.  ImcStepStats.surrogate_calls counts the queries. */
+int imc_set_surrogate(ImcHandle *h, const float *params, int64_t n_params);
+/* *active = 1 while the surrogate is on. */
+int imc_get_surrogate_active(const ImcHandle *h, int *active);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,6 +20,7 @@
 
 #include "imc.h"  // include/imc.h (on the -I path)
 #include "imc_internal.h"
+#include "imc_surrogate.cuh"
 
 using namespace imc;
 
@@ -48,6 +49,13 @@ struct ImcHandle {
     DevStats *d_stats = nullptr;
     long long stats_cap = 0;
     int grid_transport = 0, block_transport = 256, grid_emit = 0;
+    // learned surrogate: device image of the network (ca.surr_image points
+    // into it while the surrogate is on) and its kernel's persistent grid
+    void *d_surr_image = nullptr;
+    SurrWave wave{};                   // queues of the surrogate transport passes
+    std::vector<void *> qallocs;
+    long long qcap = 0;
+    SurrShapes sshape{};
     cudaGraphExec_t graph = nullptr;  // one step, captured once
     bool timing = false;
     cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -161,6 +169,36 @@ int tile_alloc(ImcHandle *h) {
 }
 
 // Grow both particle buffers so that `need` particles fit; keeps the list.
+// queues of the surrogate transport: every live history fits in each
+int surr_queue_alloc(ImcHandle *h) {
+    if (h->qcap >= h->capacity) return IMC_OK;
+    free_list(h->qallocs);
+    h->qcap = 0;
+    const long long cap = h->capacity;
+    auto take = [&](size_t bytes) -> void * {
+        void *p = nullptr;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+        h->qallocs.push_back(p);
+        return p;
+    };
+    for (SurrQueue *q : {&h->wave.q[0], &h->wave.q[1]}) {
+        q->x = (float *)take(4 * cap);
+        q->mu = (float *)take(4 * cap);
+        q->t = (float *)take(4 * cap);
+        q->E = (float *)take(4 * cap);
+        q->E0 = (float *)take(4 * cap);
+        q->cs = (int32_t *)take(4 * cap);
+        q->cs_list = (int32_t *)take(4 * cap);
+        q->idx = (long long *)take(8 * cap);
+        if (!q->x || !q->mu || !q->t || !q->E || !q->E0 || !q->cs || !q->cs_list || !q->idx) {
+            free_list(h->qallocs);
+            return fail(h, IMC_ERR_OOM, "surrogate queues");
+        }
+    }
+    h->qcap = cap;
+    return IMC_OK;
+}
+
 int grow(ImcHandle *h, long long need) {
     if (need <= h->capacity) return IMC_OK;
     long long ncap = std::max<long long>(need + need / 2, h->capacity + h->capacity / 2);
@@ -198,6 +236,7 @@ int grow(ImcHandle *h, long long need) {
     CK(h, cudaMemcpy(h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice));
     h->ca.capacity = ncap;
     if ((rc = tile_alloc(h))) return rc;
+    if (h->ca.surr_image && (rc = surr_queue_alloc(h))) return rc;
     drop_graphs(h);
     return IMC_OK;
 }
@@ -252,6 +291,12 @@ void host_timestep(const ImcDeck &d, double &t, double &dt, bool &finished) {
     finished = t > d.t_end;
 }
 
+// the transport kernel of this handle: analog, or with the learned surrogate
+void run_transport(ImcHandle *h, PBufPair bufs, cudaStream_t st) {
+    if (h->ca.surr_image) launch_transport_surr(h->ca, h->d_sc, h->prec, bufs, h->wave, h->sshape, st);
+    else launch_transport(h->ca, h->d_sc, h->prec, bufs, h->grid_transport, st);
+}
+
 // the kernel sequence of one step, asynchronous on h->stream; the list's
 // buffer is chosen on the device, so the same sequence serves every step
 int enqueue_step(ImcHandle *h, bool with_events, int ev_slot) {
@@ -260,7 +305,7 @@ int enqueue_step(ImcHandle *h, bool with_events, int ev_slot) {
     launch_update(h->ca, h->d_sc, st);
     launch_source(h->ca, h->d_sc, h->prec, bufs, h->grid_emit, st);
     if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot], st));
-    launch_transport(h->ca, h->d_sc, h->prec, bufs, h->grid_transport, st);
+    run_transport(h, bufs, st);
     if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot + 1], st));
     launch_finalize(h->ca, h->d_sc, st);
     launch_compact(h->ca, h->d_sc, h->prec, bufs, h->tile_cnt, h->tile_off, h->ntiles_cap, false, st);
@@ -506,6 +551,8 @@ int imc_destroy(ImcHandle *h) {
     for (auto e : h->ev_pool) cudaEventDestroy(e);
     for (int i = 0; i < 2; ++i) if (h->ev[i]) cudaEventDestroy(h->ev[i]);
     if (h->d_stats) cudaFree(h->d_stats);
+    if (h->d_surr_image) cudaFree(h->d_surr_image);
+    free_list(h->qallocs);
     free_list(h->pallocs);
     free_list(h->allocs);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -540,7 +587,7 @@ int imc_transport(ImcHandle *h) {
     if (!h) return IMC_ERR_INVALID_ARG;
     if (h->stage != Stage::Sourced) launch_prepare_transport(h->ca, h->d_sc, h->stream);
     if (h->timing) CK(h, cudaEventRecord(h->ev[0], h->stream));
-    launch_transport(h->ca, h->d_sc, h->prec, pair(h), h->grid_transport, h->stream);
+    run_transport(h, pair(h), h->stream);
     CKL(h);
     if (h->timing) {
         CK(h, cudaEventRecord(h->ev[1], h->stream));
@@ -948,10 +995,67 @@ int imc_transport_timing(ImcHandle *h, double *avg_ms, int64_t *launches) {
     return IMC_OK;
 }
 
+int imc_set_surrogate(ImcHandle *h, const float *params, int64_t n_params) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    if (!params) {
+        h->ca.surr_image = nullptr;
+        drop_graphs(h);
+        return IMC_OK;
+    }
+    if (n_params != surr::kParams) return fail(h, IMC_ERR_INVALID_ARG, "surrogate: expected IMC_SURROGATE_PARAMS floats");
+    if (h->geometry != IMC_GEOM_1D) return fail(h, IMC_ERR_INVALID_ARG, "surrogate: 1D geometry only");
+    if (h->prec == IMC_FP64) return fail(h, IMC_ERR_INVALID_ARG, "surrogate: FP32 or FP16 particle state only");
+    for (int64_t i = 0; i < n_params; ++i)
+        if (!std::isfinite(params[i])) return fail(h, IMC_ERR_INVALID_ARG, "surrogate: non-finite parameter");
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (!h->d_surr_image) CK(h, cudaMalloc(&h->d_surr_image, surr::kImageBytes));
+    float *dP = nullptr;
+    CK(h, cudaMalloc(&dP, sizeof(float) * surr::kParams));
+    cudaError_t e = cudaMemcpyAsync(dP, params, sizeof(float) * surr::kParams, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) {
+        launch_surr_image(dP, h->d_surr_image, h->stream);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(dP);
+    if (e != cudaSuccess) return fail(h, IMC_ERR_CUDA, std::string("surrogate image: ") + cudaGetErrorString(e));
+    CellArgs ca = h->ca;
+    ca.surr_image = reinterpret_cast<const uint4 *>(h->d_surr_image);
+    SurrShapes sh = surr_shapes(ca, h->prec);
+    if (sh.analog_smem > 227 * 1024 || sh.query_smem > 227 * 1024)
+        return fail(h, IMC_ERR_INVALID_ARG, "surrogate: mesh too large for shared memory");
+    int grids[3] = {0, 0, 0};
+    for (int which = 0; which < 3; ++which) {
+        const void *kp = surr_kernel_ptr(ca, h->prec, which);
+        const int block = which == 0 ? sh.analog_block : sh.query_block;
+        const int smem = which == 0 ? sh.analog_smem : sh.query_smem;
+        CK(h, cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        int per_sm = 0;
+        CK(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp, block, smem));
+        if (per_sm < 1) return fail(h, IMC_ERR_CUDA, "surrogate transport kernel cannot be resident");
+        grids[which] = h->sm_count * per_sm;
+    }
+    sh.analog_grid = grids[0];
+    sh.query_grid = std::min(grids[1], grids[2]);
+    int rc = surr_queue_alloc(h);
+    if (rc) return rc;
+    h->sshape = sh;
+    h->ca = ca;
+    drop_graphs(h);
+    return IMC_OK;
+}
+
+int imc_get_surrogate_active(const ImcHandle *h, int *active) {
+    if (!h || !active) return IMC_ERR_INVALID_ARG;
+    *active = h->ca.surr_image != nullptr;
+    return IMC_OK;
+}
+
 int imc_kernels_per_step(const ImcHandle *h, int *count) {
     if (!h || !count) return IMC_ERR_INVALID_ARG;
-    // update, source x5, transport, finalize, compact x4, tally, energycheck, timestep
-    *count = 15;
+    // update, source x5, transport, finalize, compact x4, tally, energycheck,
+    // timestep; the surrogate transport is 1 + kSurrRounds kernels
+    *count = 15 + (h->ca.surr_image ? kSurrRounds : 0);
     return IMC_OK;
 }
 

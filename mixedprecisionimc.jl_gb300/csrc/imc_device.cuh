@@ -28,7 +28,9 @@ constexpr uint32_t kPhiloxM1 = 0xCD9E8D57u;
 constexpr uint32_t kPhiloxW0 = 0x9E3779B9u;
 constexpr uint32_t kPhiloxW1 = 0xBB67AE85u;
 
-enum : uint32_t { kStageTransport = 0, kStageSource = 1 };
+// stream stage tags: transport, sourcing; the surrogate transport gives each
+// resumed analog pass and each query pass of round r its own stream
+enum : uint32_t { kStageTransport = 0, kStageSource = 1, kStageResume = 16, kStageQuery = 32 };
 
 IMC_HD void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
                            uint32_t out[4]) {

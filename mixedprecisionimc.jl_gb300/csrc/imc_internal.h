@@ -22,6 +22,9 @@
 
 namespace imc {
 
+// query rounds per step of the surrogate transport (launch_transport_surr)
+constexpr int kSurrRounds = 6;
+
 // scalars that live in device memory so a whole step can replay as a graph
 struct Scalars {
     double t, dt;
@@ -37,6 +40,7 @@ struct Scalars {
     double n_source;                   // particle budget of this step
     unsigned long long segments;
     unsigned long long surrogate_calls;
+    unsigned long long qcount[kSurrRounds + 1];  // surrogate transport: histories waiting for query round r
     unsigned int flags;
     int b_dep, b_rad, b_lost;          // fixed-point exponents of this transport
     unsigned int step;                 // step index (RNG key, stats slot)
@@ -71,6 +75,9 @@ struct CellArgs {
     unsigned long long seed;
     double vol_min, scale_min;
     double t_end, dtmax, kfac;
+    // learned thick-cell surrogate: tensor-core image of the network
+    // (imc_surrogate.cuh), or null for analog transport everywhere
+    const uint4 *surr_image;
 };
 
 // type-erased particle buffer
@@ -103,6 +110,34 @@ struct TransportShape {
 };
 TransportShape transport_shape(const CellArgs &ca, int prec);
 void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, int grid, cudaStream_t st);
+// 1D transport with the learned surrogate in thick cells (ca.surr_image set;
+// FP32 or FP16 state), as 1 + kSurrRounds kernels per step: an analog pass
+// over the list that sets aside the histories that want a network query,
+// then kSurrRounds query passes, each continuing its histories analog until
+// they end or want the next query.
+// histories set aside between passes (FP32 state)
+struct SurrQueue {
+    float *x, *mu, *t, *E, *E0;
+    int32_t *cs;        // cell | scale_index << 24 now
+    int32_t *cs_list;   // as stored in the list (census rewrites it on change)
+    long long *idx;     // list index
+};
+struct SurrWave {
+    SurrQueue q[2];     // round r reads q[r & 1] and fills q[(r + 1) & 1]
+};
+struct SurrShapes {
+    int analog_block, analog_smem, analog_grid;  // list pass
+    bool analog_smt;
+    int query_block, query_smem, query_grid;     // query passes
+};
+SurrShapes surr_shapes(const CellArgs &ca, int prec);
+// kernel pointers for attribute / occupancy set-up: which = 0 list pass,
+// 1 query pass that sets aside, 2 last query pass
+const void *surr_kernel_ptr(const CellArgs &ca, int prec, int which);
+void launch_transport_surr(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, const SurrWave &w,
+                           const SurrShapes &sh, cudaStream_t st);
+// writes the tensor-core image of FP32 parameters into dst (device, kImageBytes)
+void launch_surr_image(const float *params, void *dst, cudaStream_t st);
 // Removes killed particles from the list.  With force = false the list is
 // compacted only when the holes exceed 1/16 of its length (kDeferHoles);
 // otherwise the holes stay and only the live count is updated.

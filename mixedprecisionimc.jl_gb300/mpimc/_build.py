@@ -16,7 +16,8 @@ CSRC = os.path.join(PKG_ROOT, "csrc")
 BUILD = os.path.join(PKG_ROOT, "_build")
 REPO = os.path.dirname(PKG_ROOT)
 LIB = os.path.join(BUILD, "libimc.so")
-SOURCES = ["imc_api.cu", "imc_kernels.cu", "imc_transport.cu", "imc_noalloc.cu"]
+SOURCES = ["imc_api.cu", "imc_kernels.cu", "imc_transport.cu", "imc_noalloc.cu", "imc_surrogate.cu",
+           "imc_transport_surr.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--fmad=false",
               "-I", os.path.join(REPO, "include")]

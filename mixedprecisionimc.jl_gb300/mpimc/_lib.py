@@ -99,6 +99,12 @@ class ImcParticles(C.Structure):
     ]
 
 
+class ImcSurrogateTrainConfig(C.Structure):
+    """struct ImcSurrogateTrainConfig of include/imc.h."""
+    _fields_ = [("seed", C.c_uint64), ("n_samples", C.c_int64), ("batch", C.c_int32), ("iterations", C.c_int32),
+                ("lr", C.c_float), ("lr_min", C.c_float)]
+
+
 class ImcDeviceParticles(C.Structure):
     """Caller-owned device arrays for imc_clean_noalloc (device pointers)."""
     _fields_ = [("t", C.c_void_p), ("x", C.c_void_p), ("y", C.c_void_p), ("ux", C.c_void_p), ("uy", C.c_void_p),
@@ -141,6 +147,16 @@ SIGNATURES = {
     "imc_kernels_per_step": (C.c_int, [_H, C.POINTER(C.c_int)]),
     "imc_clean_noalloc": (C.c_int, [C.c_int, C.c_int, C.POINTER(ImcDeviceParticles), C.POINTER(ImcDeviceParticles),
                                     C.c_int64, C.POINTER(C.c_int64), C.c_void_p]),
+    "imc_surrogate_param_count": (C.c_int, [C.POINTER(C.c_int)]),
+    "imc_surrogate_train": (C.c_int, [C.POINTER(ImcSurrogateTrainConfig), C.c_void_p, C.c_void_p]),
+    "imc_surrogate_walk": (C.c_int, [C.c_uint64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "imc_surrogate_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                     C.POINTER(C.c_double)]),
+    "imc_surrogate_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "imc_surrogate_sample": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                       C.c_void_p]),
+    "imc_set_surrogate": (C.c_int, [_H, C.c_void_p, C.c_int64]),
+    "imc_get_surrogate_active": (C.c_int, [_H, C.POINTER(C.c_int)]),
 }
 
 _LIB = None

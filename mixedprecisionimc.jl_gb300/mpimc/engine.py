@@ -273,6 +273,21 @@ class Engine:
         self._c(self.lib.imc_get_stats(self.h, C.byref(st)))
         return st.as_dict()
 
+    def set_surrogate(self, params):
+        """Turn the learned thick-cell surrogate on (FP32 parameters from
+        mpimc.surrogate.train) or off (None); 1D, FP32 / FP16 state."""
+        import numpy as np
+        if params is None:
+            self._c(self.lib.imc_set_surrogate(self.h, None, 0))
+            return
+        P = np.ascontiguousarray(params, dtype=np.float32)
+        self._c(self.lib.imc_set_surrogate(self.h, P.ctypes.data_as(C.c_void_p), P.size))
+
+    def surrogate_active(self):
+        a = C.c_int()
+        self._c(self.lib.imc_get_surrogate_active(self.h, C.byref(a)))
+        return bool(a.value)
+
     def set_timing(self, on=True):
         self._c(self.lib.imc_set_timing(self.h, 1 if on else 0))
 

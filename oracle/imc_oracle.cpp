@@ -1083,4 +1083,50 @@ int orc_bench(const ImcDeck *deck, int nthreads, int64_t max_steps, double *seco
     return 0;
 }
 
+/* Analog in-cell walk of the learned surrogate's training data: the in-cell
+ * part of Transport.MC's loop (src/imc_transport.jl:72-193) in mean free
+ * paths -- exponential flights, isotropic re-emission (mu = 1 - 2 rand,
+ * redrawn while zero), the walk cut at path lmax.  Near face at 0, far face
+ * at d_n + d_f.  Same variates as the kernel: stream (seed, 0, i, 3). */
+int orc_surr_walk(uint64_t seed, const float *state, int64_t n, float *x, int32_t *cls, float *tgt) {
+    for (int64_t i = 0; i < n; ++i) {
+        OrcStream rs;
+        orc_stream_init(&rs, seed, 0u, (uint32_t)i, ORC_STAGE_SURR_DATA);
+        const float d_n = state[4 * i], d_f = state[4 * i + 1], lmax = state[4 * i + 3];
+        float mu = state[4 * i + 2];
+        const float W = d_n + d_f;
+        float pos = d_n, path = 0.0f, y0 = 0.0f, y1 = 0.0f;
+        int c = 2;
+        const int cap = 8 * (int)lmax + 64;
+        bool ended = false;
+        for (int it = 0; it < cap && !ended; ++it) {
+            const float s = orc_randexp_f32(&rs);
+            const float dface = mu > 0.0f ? (W - pos) / mu : pos / (-mu);
+            const float rem = lmax - path;
+            if (rem <= s && rem <= dface) {
+                pos += mu * rem;
+                y0 = (pos - d_n) / lmax; y1 = mu; c = 2; ended = true;
+            } else if (dface <= s) {
+                path += dface;
+                y0 = logf(std::max(path, 1e-30f) / lmax); y1 = fabsf(mu); c = mu > 0.0f ? 1 : 0; ended = true;
+            } else {
+                pos += mu * s;
+                path += s;
+                mu = 0.0f;
+                for (int r = 0; r < 64 && mu == 0.0f; ++r) mu = 1.0f - 2.0f * orc_rand_f32(&rs);
+                if (mu == 0.0f) mu = 1.0f;
+            }
+        }
+        if (!ended) { y0 = (pos - d_n) / lmax; y1 = mu; c = 2; }
+        x[4 * i] = d_n < lmax ? d_n / lmax : 1.0f;
+        x[4 * i + 1] = d_f < lmax ? d_f / lmax : 1.0f;
+        x[4 * i + 2] = state[4 * i + 2];
+        x[4 * i + 3] = (log10f(lmax) - 2.0f) * 0.5f;
+        cls[i] = c;
+        tgt[2 * i] = y0;
+        tgt[2 * i + 1] = y1;
+    }
+    return 0;
+}
+
 }  // extern "C"

@@ -60,6 +60,7 @@ def load():
                                     C.POINTER(C.c_double), C.POINTER(C.c_int)]),
         "orc_bench": (C.c_int, [C.POINTER(ImcDeck), C.c_int, C.c_int64, C.POINTER(C.c_double),
                                 C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+        "orc_surr_walk": (C.c_int, [C.c_uint64, V, C.c_int64, V, V, V]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -76,6 +77,30 @@ def philox(ctr, key):
     o = (C.c_uint32 * 4)()
     lib.orc_philox(c, k, o)
     return list(o)
+
+
+def surr_walk(seed, state):
+    """CPU restatement of the surrogate's analog in-cell walk at the given
+    (d_n, d_f, mu', lmax) rows: (x, cls, tgt) like imc_surrogate_walk."""
+    lib = load()
+    st = np.ascontiguousarray(state, dtype=np.float32)
+    n = len(st)
+    x = np.zeros((n, 4), np.float32)
+    cls = np.zeros(n, np.int32)
+    tgt = np.zeros((n, 2), np.float32)
+    lib.orc_surr_walk(seed, st.ctypes.data_as(C.c_void_p), n, x.ctypes.data_as(C.c_void_p),
+                      cls.ctypes.data_as(C.c_void_p), tgt.ctypes.data_as(C.c_void_p))
+    return x, cls, tgt
+
+
+def philox_uniforms(seed, step, index, stage, count):
+    """The first `count` FP32 uniforms of the kernels' stream (seed, step, index, stage)."""
+    words = []
+    blk = 0
+    while len(words) < count:
+        words += philox([blk, step, index, stage], [seed & 0xFFFFFFFF, seed >> 32])
+        blk += 1
+    return [float(w >> 8) * 2.0 ** -24 for w in words[:count]]
 
 
 def sorter(vals, scales, prec=0):

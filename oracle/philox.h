@@ -21,7 +21,7 @@
 #define ORC_PHILOX_W0 0x9E3779B9u
 #define ORC_PHILOX_W1 0xBB67AE85u
 
-enum { ORC_STAGE_TRANSPORT = 0, ORC_STAGE_SOURCE = 1 };
+enum { ORC_STAGE_TRANSPORT = 0, ORC_STAGE_SOURCE = 1, ORC_STAGE_SURR_DATA = 3, ORC_STAGE_SURR_TEST = 4 };
 
 static inline void orc_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4]) {
     uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];

@@ -63,6 +63,14 @@ def test_c2_fp32_ensemble_mean_matches_fp64_mean(gpu_lib):
         T.append(e.field("temp"))
         e.close()
     T = np.array(T)
-    z = (T.mean(0) - g["temp"]) / np.sqrt(T.std(0, ddof=1) ** 2 / len(T) + g["temp_std"] ** 2 / len(g["seeds"]))
+    # Under "FP32 state = FP64 state in distribution" both ensembles share the
+    # per-cell variance; the 32-run estimate is used for both, so z is close to
+    # Student-t with 31 degrees of freedom (E z^2 = 31/29).  The 8-run sample
+    # variance would make it t with 7 (E z^2 = 7/5) and hide a bias.
+    live = g["temp_std"] > 0
+    z = (T.mean(0) - g["temp"])[live] / (g["temp_std"][live] * np.sqrt(1.0 / len(T) + 1.0 / len(g["seeds"])))
     assert np.mean(np.abs(z) < 3.0) >= 0.98, np.sort(np.abs(z))[-10:]
-    assert np.mean(z ** 2) < 1.3, np.mean(z ** 2)
+    # neighbouring cells are correlated (a few hundred independent values)
+    assert np.mean(z ** 2) < 1.5, np.mean(z ** 2)
+    # a systematic shift of the whole profile
+    assert abs(np.mean(z)) < 0.5, np.mean(z)
