@@ -14,6 +14,11 @@ One bench step is one full simulation (t = 0 -> 3).  Printed on one JSON line:
   fp64         the same deck with FP64 particle state (the plain FP64 GPU
                path), as many runs as the timed steps: segments/s, relerr, FOM
   fp16_state   one run with binary16 particle state
+  learned      the learned thick-cell surrogate (trained first, on the GPU)
+               with FP32 state on the thick-slab deck against plain FP32 and
+               plain FP64, relerr against tests/golden/thick_fp64_mean.npz
+  c3           the nonlinear heat wave, FP32 state against plain FP64,
+               relerr against tests/golden/c3_fp64_mean.npz
   e2e          segments/s through the public API with host buffers: deck
                upload, run and the read-back of the cell fields per step
   roofline     the transport kernel: algorithmic bytes per launch over its
@@ -175,6 +180,82 @@ def run_once(inputs, mesh, overrides=None, timing=False):
             "energy_error": max(abs(s["energy_error"]) for s in steps)}
 
 
+def deck_runs(deck_file, offsets, overrides=None, params=None):
+    """Full simulations of a test deck (seeds SEED + offset) on the GPU, with
+    the learned surrogate when params is given."""
+    import mpimc
+    out = []
+    for off in offsets:
+        inputs = mpimc.Input.readInputs(os.path.join(GOLDEN, "decks", deck_file))
+        inputs["SEED"] = str(int(inputs["SEED"]) + off)
+        mesh = mpimc.Mesh.mesh_generation(inputs)
+        eng = mpimc.Engine(inputs, mesh, overrides)
+        try:
+            if params is not None:
+                eng.set_surrogate(params)
+            steps, ms = eng.run()
+            temp = eng.field("temp")
+            kps = eng.kernels_per_step()
+        finally:
+            eng.close()
+        out.append({"ms": ms, "temp": temp, "segments": sum(s["segments"] for s in steps),
+                    "calls": sum(s["surrogate_calls"] for s in steps), "kernels": kps * len(steps),
+                    "energy_error": max([abs(s["energy_error"]) for s in steps[:-1]] or [0.0])})
+    return out
+
+
+def summarize(runs, ref):
+    """ms per run, RMS relative temperature error against the FP64 mean,
+    FOM = 1/(relerr^2 s), analog segments and surrogate queries per run."""
+    import numpy as np
+    secs = sum(r["ms"] for r in runs) / 1000.0 / len(runs)
+    rel = float(np.sqrt(np.mean([relerr(r["temp"], ref) ** 2 for r in runs])))
+    return {"runs": len(runs), "ms_per_run": 1000.0 * secs, "relerr_T": rel, "fom": 1.0 / (rel ** 2 * secs),
+            "segments_per_run": float(np.mean([r["segments"] for r in runs])),
+            "surrogate_calls_per_run": float(np.mean([r["calls"] for r in runs])),
+            "energy_error_max": max(r["energy_error"] for r in runs)}
+
+
+def fp64_ref(name):
+    import numpy as np
+    return np.load(os.path.join(GOLDEN, name + "_fp64_mean.npz"))
+
+
+def learned_section(n):
+    """The learned part on the thick-slab deck (40 mean free paths per cell):
+    learned surrogate + FP32 state against plain FP32 and plain FP64, each
+    against the 32-seed FP64 mean; the network is trained here first."""
+    from mpimc import surrogate
+    t0 = time.perf_counter()
+    P = surrogate.train()
+    train_s = time.perf_counter() - t0
+    ref = fp64_ref("thick")
+    learned = summarize(deck_runs("thick_slab.txt", range(1, n + 1), None, P), ref)
+    fp32 = summarize(deck_runs("thick_slab.txt", range(101, n + 101)), ref)
+    fp64 = summarize(deck_runs("thick_slab.txt", range(201, n + 201), {"precision": 0, "scale_select_precision": 0}),
+                     ref)
+    return {"deck": "thick_slab.txt",
+            "workload": "1D linearized thick slab, 30 cells of 40 mean free paths (sigma_a=800, dx=0.05), "
+                        "source on [0,0.5], dt=0.5 to t=10, NINPUT=2e5, NMAX=2e6",
+            "train_s": train_s, "train": dict(surrogate.DEFAULT_TRAIN),
+            "learned_fp32": learned, "fp32": fp32, "fp64": fp64,
+            "fom_ratio_learned_over_fp64": learned["fom"] / fp64["fom"],
+            "fom_ratio_learned_over_fp32": learned["fom"] / fp32["fom"],
+            "segment_ratio_fp32_over_learned": fp32["segments_per_run"] / learned["segments_per_run"]}
+
+
+def c3_section(n):
+    """The nonlinear heat wave (the surrogate's gate stays closed there: its
+    thick cells never hold walks of 100 collisions) -- FP32 state against
+    plain FP64, against the 32-seed FP64 mean."""
+    ref = fp64_ref("c3")
+    fp32 = summarize(deck_runs("c3_heatwave.txt", range(1, n + 1)), ref)
+    fp64 = summarize(deck_runs("c3_heatwave.txt", range(101, n + 101), {"precision": 0, "scale_select_precision": 0}),
+                     ref)
+    return {"deck": "c3_heatwave.txt", "workload": DECKS["c3"][1], "fp32": fp32, "fp64": fp64,
+            "fom_ratio_fp32_over_fp64": fp32["fom"] / fp64["fom"]}
+
+
 def e2e_once(seed_offset):
     """Public-API run with host buffers: build the deck on the host, create the
     engine (uploads it), run, read the cell fields back, destroy."""
@@ -266,6 +347,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp16", action="store_true", help="skip the FP16-state run")
     ap.add_argument("--deck", default="c2", choices=sorted(DECKS), help="workload (c2 is the headline)")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-surrogate comparison (thick slab)")
+    ap.add_argument("--no-c3", action="store_true", help="skip the nonlinear heat-wave FP32 / FP64 comparison")
     ap.add_argument("--profile", action="store_true",
                     help="profiling case for ncu: the deck at half the particle counts, 12 timesteps, then exit")
     args = ap.parse_args()
@@ -366,6 +449,10 @@ def main():
         out["time_ratio_fp64_over_fp32"] = out["fp64"]["ms_per_step"] / (dev_ms / args.steps)
     if not args.no_fp16:
         out["fp16_state"] = comparator(2, 11, 1)
+    if not args.no_learned:
+        out["learned"] = learned_section(max(args.steps, 4))
+    if not args.no_c3:
+        out["c3"] = c3_section(2)
     w, s, h2d, d2h = e2e_once(2000)
     out["e2e"] = {"value": s / w, "unit": "segments/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                   "wall_s_per_step": w}

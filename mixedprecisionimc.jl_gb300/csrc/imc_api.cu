@@ -181,7 +181,7 @@ int surr_queue_alloc(ImcHandle *h) {
         h->qallocs.push_back(p);
         return p;
     };
-    for (SurrQueue *q : {&h->wave.q[0], &h->wave.q[1]}) {
+    for (SurrQueue *q : {&h->wave.ask, &h->wave.resume}) {
         q->x = (float *)take(4 * cap);
         q->mu = (float *)take(4 * cap);
         q->t = (float *)take(4 * cap);
@@ -1024,19 +1024,19 @@ int imc_set_surrogate(ImcHandle *h, const float *params, int64_t n_params) {
     SurrShapes sh = surr_shapes(ca, h->prec);
     if (sh.analog_smem > 227 * 1024 || sh.query_smem > 227 * 1024)
         return fail(h, IMC_ERR_INVALID_ARG, "surrogate: mesh too large for shared memory");
-    int grids[3] = {0, 0, 0};
-    for (int which = 0; which < 3; ++which) {
+    int grids[4] = {0, 0, 0, 0};
+    for (int which = 0; which < 4; ++which) {
         const void *kp = surr_kernel_ptr(ca, h->prec, which);
-        const int block = which == 0 ? sh.analog_block : sh.query_block;
-        const int smem = which == 0 ? sh.analog_smem : sh.query_smem;
+        const int block = which == 3 ? sh.query_block : sh.analog_block;
+        const int smem = which == 3 ? sh.query_smem : sh.analog_smem;
         CK(h, cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         int per_sm = 0;
         CK(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp, block, smem));
         if (per_sm < 1) return fail(h, IMC_ERR_CUDA, "surrogate transport kernel cannot be resident");
         grids[which] = h->sm_count * per_sm;
     }
-    sh.analog_grid = grids[0];
-    sh.query_grid = std::min(grids[1], grids[2]);
+    sh.analog_grid = std::min(grids[0], std::min(grids[1], grids[2]));
+    sh.query_grid = grids[3];
     int rc = surr_queue_alloc(h);
     if (rc) return rc;
     h->sshape = sh;
@@ -1054,8 +1054,8 @@ int imc_get_surrogate_active(const ImcHandle *h, int *active) {
 int imc_kernels_per_step(const ImcHandle *h, int *count) {
     if (!h || !count) return IMC_ERR_INVALID_ARG;
     // update, source x5, transport, finalize, compact x4, tally, energycheck,
-    // timestep; the surrogate transport is 1 + kSurrRounds kernels
-    *count = 15 + (h->ca.surr_image ? kSurrRounds : 0);
+    // timestep; the surrogate transport is 1 + 2 kSurrRounds kernels
+    *count = 15 + (h->ca.surr_image ? 2 * kSurrRounds : 0);
     return IMC_OK;
 }
 

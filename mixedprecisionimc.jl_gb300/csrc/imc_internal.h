@@ -23,7 +23,7 @@
 namespace imc {
 
 // query rounds per step of the surrogate transport (launch_transport_surr)
-constexpr int kSurrRounds = 6;
+constexpr int kSurrRounds = 1;  // measured best on GB300: each further round costs a pass whose tail outweighs its queries
 
 // scalars that live in device memory so a whole step can replay as a graph
 struct Scalars {
@@ -40,7 +40,7 @@ struct Scalars {
     double n_source;                   // particle budget of this step
     unsigned long long segments;
     unsigned long long surrogate_calls;
-    unsigned long long qcount[kSurrRounds + 1];  // surrogate transport: histories waiting for query round r
+    unsigned long long qcount[2 * kSurrRounds + 1];  // surrogate transport: ask queue of round r at 2r, resume queue at 2r + 1
     unsigned int flags;
     int b_dep, b_rad, b_lost;          // fixed-point exponents of this transport
     unsigned int step;                 // step index (RNG key, stats slot)
@@ -111,10 +111,9 @@ struct TransportShape {
 TransportShape transport_shape(const CellArgs &ca, int prec);
 void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, int grid, cudaStream_t st);
 // 1D transport with the learned surrogate in thick cells (ca.surr_image set;
-// FP32 or FP16 state), as 1 + kSurrRounds kernels per step: an analog pass
+// FP32 or FP16 state), as 1 + 2 kSurrRounds kernels per step: an analog pass
 // over the list that sets aside the histories that want a network query,
-// then kSurrRounds query passes, each continuing its histories analog until
-// they end or want the next query.
+// then rounds of (query pass, analog pass over the continuing histories).
 // histories set aside between passes (FP32 state)
 struct SurrQueue {
     float *x, *mu, *t, *E, *E0;
@@ -123,7 +122,8 @@ struct SurrQueue {
     long long *idx;     // list index
 };
 struct SurrWave {
-    SurrQueue q[2];     // round r reads q[r & 1] and fills q[(r + 1) & 1]
+    SurrQueue ask;      // waiting for a query
+    SurrQueue resume;   // continuing after a query
 };
 struct SurrShapes {
     int analog_block, analog_smem, analog_grid;  // list pass
@@ -132,7 +132,7 @@ struct SurrShapes {
 };
 SurrShapes surr_shapes(const CellArgs &ca, int prec);
 // kernel pointers for attribute / occupancy set-up: which = 0 list pass,
-// 1 query pass that sets aside, 2 last query pass
+// 1 resume pass that sets aside, 2 last resume pass, 3 query pass
 const void *surr_kernel_ptr(const CellArgs &ca, int prec, int which);
 void launch_transport_surr(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, const SurrWave &w,
                            const SurrShapes &sh, cudaStream_t st);

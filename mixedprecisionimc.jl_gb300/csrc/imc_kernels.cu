@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_source_scan(CellArgs ca, Scala
         sc->emax_census_bits = 0ull;
         sc->segments = 0ull;
         sc->surrogate_calls = 0ull;
-        for (int r = 0; r <= kSurrRounds; ++r) sc->qcount[r] = 0ull;
+        for (int r = 0; r <= 2 * kSurrRounds; ++r) sc->qcount[r] = 0ull;
         sc->b_dep = fix_exponent(emax / ca.vol_min);
         sc->b_lost = fix_exponent(emax);
         sc->b_rad = fix_exponent(emax);
@@ -840,7 +840,7 @@ __global__ void k_prepare_transport(CellArgs ca, Scalars *sc) {
     sc->emax_census_bits = 0ull;
     sc->segments = 0ull;
     sc->surrogate_calls = 0ull;
-    for (int r = 0; r <= kSurrRounds; ++r) sc->qcount[r] = 0ull;
+    for (int r = 0; r <= 2 * kSurrRounds; ++r) sc->qcount[r] = 0ull;
     sc->n_census_in = sc->n_census;
     sc->n_sourced = 0;
     sc->birth_base = sc->n_particles;

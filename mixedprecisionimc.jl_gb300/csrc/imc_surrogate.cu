@@ -37,7 +37,9 @@ constexpr int kWalkCapFactor = 8;        // flight cap: 8 * lmax + 64
 
 // ----------------------------------------------------------- in-cell walk
 // Analog walk from (d_n, d_f, mu', lmax), all in mean free paths, near face at
-// 0, far face at d_n + d_f.  Returns the outcome and the two targets.
+// 0, far face at d_n + d_f.  Returns the outcome and the two targets: for an
+// exit ln(path / lmax) and |mu|, for truncation the displacement toward the
+// far face / sqrt(lmax) and the final mu'.
 __device__ int walk(Stream &rs, float d_n, float d_f, float mu, float lmax, float *y0, float *y1) {
     const float W = d_n + d_f;
     float pos = d_n, path = 0.0f;
@@ -48,7 +50,7 @@ __device__ int walk(Stream &rs, float d_n, float d_f, float mu, float lmax, floa
         const float rem = lmax - path;
         if (rem <= s && rem <= dface) {
             pos += mu * rem;
-            *y0 = (pos - d_n) / lmax;
+            *y0 = (pos - d_n) / sqrtf(lmax);
             *y1 = mu;
             return kTrunc;
         }
@@ -64,7 +66,7 @@ __device__ int walk(Stream &rs, float d_n, float d_f, float mu, float lmax, floa
         for (int r = 0; r < 64 && mu == 0.0f; ++r) mu = 1.0f - 2.0f * Rand<float>::u(rs);
         if (mu == 0.0f) mu = 1.0f;
     }
-    *y0 = (pos - d_n) / lmax;
+    *y0 = (pos - d_n) / sqrtf(lmax);
     *y1 = mu;
     return kTrunc;
 }

@@ -18,12 +18,15 @@
 //
 // The network (4 inputs, three hidden layers of 64 ReLU units, 64 outputs;
 // BF16 weights in the transport kernel, FP32 accumulation) maps
-//   x = (min(d_n/lmax, 1), min(d_f/lmax, 1), mu', (log10 lmax - 2)/2)
-// to the logits of the three outcomes and, for each outcome, the quantiles of
-// its conditional distributions, sampled by inverse transform:
+//   x = (g(d_n / sqrt(lmax)), g(d_f / sqrt(lmax)), mu', (log10 lmax - 2)/2),
+//   g(r) = min(ln(1 + r) / ln 11, 1),
+// -- distances in diffusion lengths, which decide whether a face is within
+// reach; ten or more are as good as infinity -- to the logits of the three
+// outcomes and, for each outcome, the quantiles of its conditional
+// distributions, sampled by inverse transform:
 //   near / far exit:  y = ln(l / lmax) (12 quantiles), exit |mu| (6)
-//   truncation:       displacement (x_end - x_start)/lmax toward the far face (6),
-//                     final mu' (6)
+//   truncation:       displacement (x_end - x_start)/sqrt(lmax) toward the far
+//                     face (6), final mu' (6)
 // Quantile heads are monotone by construction: q_0 = h_0,
 // q_k = q_{k-1} + softplus(h_k).
 #pragma once
@@ -71,9 +74,13 @@ constexpr float kCellMin = 8.0f;             // cell at least this many mfp wide
 constexpr float kMinGain = 100.0f;           // ask only if the walk would take this many collisions
 
 // network input from the walk's dimensionless state
+IMC_HD float reach(float d, float lmax) {
+    const float v = log1pf(d / sqrtf(lmax)) * 0.41703239f;  // 1 / ln 11
+    return v < 1.0f ? v : 1.0f;
+}
 IMC_HD void features(float d_n, float d_f, float mu_p, float lmax, float x[kIn]) {
-    x[0] = d_n < lmax ? d_n / lmax : 1.0f;
-    x[1] = d_f < lmax ? d_f / lmax : 1.0f;
+    x[0] = reach(d_n, lmax);
+    x[1] = reach(d_f, lmax);
     x[2] = mu_p;
     x[3] = (log10f(lmax) - 2.0f) * 0.5f;
 }

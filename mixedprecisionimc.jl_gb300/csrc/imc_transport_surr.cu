@@ -236,7 +236,7 @@ __device__ __forceinline__ int apply_outcome(const CellArgs &ca, const Tab1<T> *
     T dist, xn, mun;
     bool face = false;
     if (cls == kTrunc) {
-        const float pos = fminf(fmaxf(q.dn + y0 * q.L, 0.0f), q.W);  // from the near face
+        const float pos = fminf(fmaxf(q.dn + y0 * sqrtf(q.L), 0.0f), q.W);  // from the near face
         const float xm = q.near_left ? pos : q.W - pos;
         xn = (T)(xm / seff);
         xn = xn < (T)0 ? (T)0 : (xn > ce.dxs ? ce.dxs : xn);
@@ -317,19 +317,36 @@ __device__ __forceinline__ void fill_table(const CellArgs &ca, Tab1<T> *tab, T d
     }
 }
 
+// Per-cell gate of the analog passes: 0 where no history can want a query
+// this step -- cell narrower than kCellMin mean free paths, or lmax below
+// kMinGain even at the step's start with full energy (census path
+// seff c dt ds, cut-off path ln(100) seff / (sigma_a f)).
+template <class T>
+__device__ __forceinline__ void fill_gate(const CellArgs &ca, uint8_t *gate, T ds, T c, T dt) {
+    for (int i = threadIdx.x; i < ca.nx; i += blockDim.x) {
+        const float sa = (float)ca.sa[i], f = (float)ca.fleck[i], ss = (float)ca.ss[i];
+        const float saf = sa * f, seff = sa * (1.0f - f) + ss;
+        const float W = (float)ca.dx[i] * (float)ds * seff;
+        const float lcen = seff * (float)(c * dt * ds);
+        const float lcut = saf > 0.0f ? 4.6051702f * seff / saf : INFINITY;
+        gate[i] = (W >= kCellMin && fminf(lcen, lcut) >= kMinGain) ? 1 : 0;
+    }
+}
+
 // Walks a history analog until it ends (kCensus / kKilled) or, with pause,
 // until it wants a query (kPaused, its deposits flushed).  A certain kill ends
 // it at once.
 template <class T, bool SMT>
-__device__ __forceinline__ int walk_analog(const CellArgs &ca, const Tab1<T> *tab, Hist<T> &h, bool pause, T c, T ds,
+__device__ __forceinline__ int walk_analog(const CellArgs &ca, const Tab1<T> *tab, const uint8_t *gate, Hist<T> &h,
+                                           bool pause, T c, T ds,
                                            bool ds_one, T dt, long long cap, int N, bool reflect_l, bool reflect_r,
                                            long long *dep_acc, int nc, int b_dep, int b_lost, unsigned &flags,
                                            unsigned long long &calls) {
     int res = kGo;
     while (true) {
-        if (pause) {
+        if (pause && gate[h.cell]) {
             const Tab1<T> ce = tab[h.cell];
-            if (ce.dxs * ce.seff >= (T)kCellMin) {
+            {
                 Query q;
                 const int kind = decide<T>(ce, h, c, ds, dt, q);
                 if (kind == kCertainKill) {
@@ -356,12 +373,16 @@ __device__ __forceinline__ int walk_analog(const CellArgs &ca, const Tab1<T> *ta
     return res;
 }
 
-// -------------------------------------------------------------- list pass
-// The analog kernel over the particle list; a history that wants a query is
-// set aside in queue 0.
-template <class St, int BLOCK, bool SMT>
-__global__ void __launch_bounds__(BLOCK) k_wave_list(CellArgs ca, Scalars *sc, PBufPair bufs, SurrWave w) {
+// ------------------------------------------------------------ analog pass
+// The analog kernel over the list (IN_Q = false; its pauses fill the ask
+// queue of round 0) or over the resume queue of round `round` (IN_Q = true;
+// with PAUSE its pauses fill the ask queue of round + 1).
+template <class St, int BLOCK, bool SMT, bool IN_Q, bool PAUSE>
+__global__ void __launch_bounds__(BLOCK) k_wave_analog(CellArgs ca, Scalars *sc, PBufPair bufs, SurrWave w,
+                                                       int round) {
     typedef typename St::T T;
+    const long long n = IN_Q ? (long long)sc->qcount[2 * round + 1] : sc->n_particles;
+    if (n == 0) return;
     PBuf<St> pb(bufs.b[sc->cur]);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Tab1<T> *tab = reinterpret_cast<Tab1<T> *>(smem_raw);
@@ -374,10 +395,13 @@ __global__ void __launch_bounds__(BLOCK) k_wave_list(CellArgs ca, Scalars *sc, P
         rad_acc = dep_acc + 3 * (size_t)ca.K * ca.nc;
         for (int i = threadIdx.x; i < 6 * ca.K * ca.nc; i += blockDim.x) dep_acc[i] = 0;
     }
-    fill_table<T>(ca, tab, ds);
-    __syncthreads();
     const T dt = (T)sc->dt;
-    const long long n = sc->n_particles;
+    uint8_t *gate = smem_raw + table_bytes(ca, sizeof(T)) + (SMT ? 6 * 8 * ca.K * ca.nc : 0);
+    fill_table<T>(ca, tab, ds);
+    fill_gate<T>(ca, gate, ds, c, dt);
+    __syncthreads();
+    unsigned long long *ask_count = &sc->qcount[IN_Q ? 2 * round + 2 : 0];
+    const uint32_t stage = kStageResume + (uint32_t)round;
     const int b_dep = sc->b_dep, b_rad = sc->b_rad, b_lost = sc->b_lost;
     const unsigned step = sc->step;
     const unsigned long long seed = ca.seed;
@@ -387,15 +411,19 @@ __global__ void __launch_bounds__(BLOCK) k_wave_list(CellArgs ca, Scalars *sc, P
     unsigned flags = 0;
     T emax = (T)0;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        if (!pb.alive[i]) continue;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
         Hist<T> h;
-        load_hist<St, T>(pb, tab, i, dt, seed, step, h);
-        const int res = walk_analog<T, SMT>(ca, tab, h, true, c, ds, ds_one, dt, cap, N, reflect_l, reflect_r,
+        if (IN_Q) {
+            load_queued<T>(w.resume, e, seed, step, stage, h);
+        } else {
+            if (!pb.alive[e]) continue;
+            load_hist<St, T>(pb, tab, e, dt, seed, step, h);
+        }
+        const int res = walk_analog<T, SMT>(ca, tab, gate, h, PAUSE, c, ds, ds_one, dt, cap, N, reflect_l, reflect_r,
                                             dep_acc, nc, b_dep, b_lost, flags, calls);
-        if (res == kPaused) store_queued<T>(w.q[0], atomicAdd(&sc->qcount[0], 1ull), h);
+        if (res == kPaused) store_queued<T>(w.ask, atomicAdd(ask_count, 1ull), h);
         else if (res == kCensus) census<St, T, SMT>(pb, tab, h, rad_acc, nc, b_rad, flags, emax);
-        else pb.alive[i] = 0;
+        else pb.alive[h.i] = 0;
         segs += (unsigned long long)h.seg;
     }
     if (SMT) flush_block_tallies(ca, dep_acc);
@@ -405,15 +433,15 @@ __global__ void __launch_bounds__(BLOCK) k_wave_list(CellArgs ca, Scalars *sc, P
 }
 
 // ------------------------------------------------------------- query pass
-// Query round `round`: every history of queue round & 1 gets one network
-// query (32 histories per warp, two tensor-core passes of 16 rows), then
-// walks on analog until it ends or (PAUSE) wants the next query, which sets
-// it aside in the other queue for the next round.
-template <class St, bool PAUSE>
+// One network query for every history of the ask queue of round `round`:
+// 32 histories per warp, two tensor-core passes of 16 rows, all lanes
+// sampling.  Census, kill and escape end the history; face exits and
+// 1e4-path pieces continue in the resume queue.
+template <class St>
 __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scalars *sc, PBufPair bufs, SurrWave w,
-                                                            int round) {
+                                                               int round) {
     typedef float T;
-    const long long n = (long long)sc->qcount[round];
+    const long long n = (long long)sc->qcount[2 * round];
     if (n == 0) return;
     PBuf<St> pb(bufs.b[sc->cur]);
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -432,18 +460,18 @@ __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scal
     fill_table<T>(ca, tab, ds);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
     float *xin = stage_all + warp * kStageFloats;
     float *yout = xin + 16 * kIn;
     const T dt = (T)sc->dt;
-    const SurrQueue qin = w.q[round & 1], qout = w.q[(round + 1) & 1];
-    unsigned long long *out_count = &sc->qcount[round + 1];
+    unsigned long long *resume_count = &sc->qcount[2 * round + 1];
     const uint32_t stage = kStageQuery + (uint32_t)round;
     const int b_dep = sc->b_dep, b_rad = sc->b_rad, b_lost = sc->b_lost;
     const unsigned step = sc->step;
     const unsigned long long seed = ca.seed;
     const long long cap = ca.seg_cap;
     const bool reflect_r = ca.bc[1] == 1, reflect_l = ca.bc[0] == 1;
-    unsigned long long segs = 0, calls = 0;
+    unsigned long long calls = 0;
     unsigned flags = 0;
     T emax = (T)0;
     const long long wstride = (long long)gridDim.x * kQueryWarps * 32;
@@ -454,7 +482,7 @@ __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scal
         Query q;
         int kind = kAnalog;
         if (valid) {
-            load_queued<T>(qin, e, seed, step, stage, h);
+            load_queued<T>(w.ask, e, seed, step, stage, h);
             kind = decide<T>(tab[h.cell], h, c, ds, dt, q);  // the state the history was set aside with
         }
         int cls = kTrunc;
@@ -474,8 +502,8 @@ __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scal
             }
             __syncwarp();
         }
+        int res = kGo;
         if (valid) {
-            int res = kGo;
             if (kind == kAsk) {
                 res = apply_outcome<T>(ca, tab, h, q, cls, y0, y1, c, ds, ds_one, dt, cap, N, reflect_l, reflect_r,
                                        b_lost, flags);
@@ -485,20 +513,24 @@ __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scal
                 calls += 1;
                 res = kKilled;
             }
-            if (res == kGo)
-                res = walk_analog<T, false>(ca, tab, h, PAUSE, c, ds, ds_one, dt, cap, N, reflect_l, reflect_r,
-                                            ca.dep_acc, nc, b_dep, b_lost, flags, calls);
-            else
-                flush_pair<T, false>(ca.dep_acc, h.k * nc + h.acc_cell, h.acc_s, h.acc_c, b_dep, flags);
-            if (res == kPaused) store_queued<T>(qout, atomicAdd(out_count, 1ull), h);
-            else if (res == kCensus) census<St, T, false>(pb, tab, h, ca.rad_acc, nc, b_rad, flags, emax);
-            else pb.alive[h.i] = 0;
-            segs += (unsigned long long)h.seg;
+            flush_pair<T, false>(ca.dep_acc, h.k * nc + h.acc_cell, h.acc_s, h.acc_c, b_dep, flags);
+            if (res == kCensus) census<St, T, false>(pb, tab, h, ca.rad_acc, nc, b_rad, flags, emax);
+            else if (res == kKilled) pb.alive[h.i] = 0;
+        }
+        // continuing histories go to the resume queue, one atomic per warp
+        const bool go = valid && res == kGo;
+        const unsigned m = __ballot_sync(kFull, go);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            unsigned long long b0 = 0;
+            if (lane == leader) b0 = atomicAdd(resume_count, (unsigned long long)__popc(m));
+            b0 = __shfl_sync(kFull, b0, leader);
+            if (go) store_queued<T>(w.resume, b0 + __popc(m & lt), h);
         }
     }
     for (int off = 16; off > 0; off >>= 1) calls += __shfl_down_sync(kFull, calls, off);
     if (lane == 0 && calls) atomicAdd(&sc->surrogate_calls, calls);
-    finish_counters<T>(sc, segs, flags, emax);
+    finish_counters<T>(sc, 0ull, flags, emax);
 }
 
 // BF16 fragment image of FP32 parameters (one block)
@@ -513,20 +545,23 @@ __global__ void k_surr_image(const float *P, uint4 *dst) {
 }
 
 template <class St, int B, bool SMT>
-void launch_wave(const CellArgs &ca, Scalars *sc, PBufPair bufs, const SurrWave &w, const SurrShapes &sh,
-                 cudaStream_t st) {
-    k_wave_list<St, B, SMT><<<sh.analog_grid, B, sh.analog_smem, st>>>(ca, sc, bufs, w);
-    for (int r = 0; r < kSurrRounds; ++r) {
-        if (r + 1 < kSurrRounds)
-            k_wave_query<St, true><<<sh.query_grid, kQueryBlock, sh.query_smem, st>>>(ca, sc, bufs, w, r);
-        else
-            k_wave_query<St, false><<<sh.query_grid, kQueryBlock, sh.query_smem, st>>>(ca, sc, bufs, w, r);
-    }
+const void *analog_ptr(int which) {
+    if (which == 0) return (const void *)k_wave_analog<St, B, SMT, false, true>;
+    if (which == 1) return (const void *)k_wave_analog<St, B, SMT, true, true>;
+    return (const void *)k_wave_analog<St, B, SMT, true, false>;
 }
 
-template <class St>
-const void *query_ptr(int which) {
-    return which == 1 ? (const void *)k_wave_query<St, true> : (const void *)k_wave_query<St, false>;
+template <class St, int B, bool SMT>
+void launch_wave(const CellArgs &ca, Scalars *sc, PBufPair bufs, const SurrWave &w, const SurrShapes &sh,
+                 cudaStream_t st) {
+    k_wave_analog<St, B, SMT, false, true><<<sh.analog_grid, B, sh.analog_smem, st>>>(ca, sc, bufs, w, 0);
+    for (int r = 0; r < kSurrRounds; ++r) {
+        k_wave_query<St><<<sh.query_grid, kQueryBlock, sh.query_smem, st>>>(ca, sc, bufs, w, r);
+        if (r + 1 < kSurrRounds)
+            k_wave_analog<St, B, SMT, true, true><<<sh.analog_grid, B, sh.analog_smem, st>>>(ca, sc, bufs, w, r);
+        else
+            k_wave_analog<St, B, SMT, true, false><<<sh.analog_grid, B, sh.analog_smem, st>>>(ca, sc, bufs, w, r);
+    }
 }
 
 }  // namespace
@@ -535,7 +570,7 @@ SurrShapes surr_shapes(const CellArgs &ca, int prec) {
     SurrShapes s{};
     const TransportShape ts = transport_shape(ca, prec);
     s.analog_block = ts.block;
-    s.analog_smem = ts.smem;
+    s.analog_smem = ts.smem + ((ca.nx + 15) & ~15);  // + the per-cell gate
     s.analog_smt = ts.smem_tally;
     s.query_block = kQueryBlock;
     s.query_smem = kQueryHead + table_bytes(ca, 4);
@@ -544,9 +579,9 @@ SurrShapes surr_shapes(const CellArgs &ca, int prec) {
 
 const void *surr_kernel_ptr(const CellArgs &ca, int prec, int which) {
     const bool smt = transport_shape(ca, prec).smem_tally;
-    if (which != 0) return prec == 2 ? query_ptr<StF16>(which) : query_ptr<StF32>(which);
-    if (prec == 2) return smt ? (const void *)k_wave_list<StF16, 768, true> : (const void *)k_wave_list<StF16, 256, false>;
-    return smt ? (const void *)k_wave_list<StF32, 768, true> : (const void *)k_wave_list<StF32, 256, false>;
+    if (which == 3) return prec == 2 ? (const void *)k_wave_query<StF16> : (const void *)k_wave_query<StF32>;
+    if (prec == 2) return smt ? analog_ptr<StF16, 768, true>(which) : analog_ptr<StF16, 256, false>(which);
+    return smt ? analog_ptr<StF32, 768, true>(which) : analog_ptr<StF32, 256, false>(which);
 }
 
 void launch_transport_surr(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, const SurrWave &w,

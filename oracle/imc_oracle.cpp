@@ -1105,7 +1105,7 @@ int orc_surr_walk(uint64_t seed, const float *state, int64_t n, float *x, int32_
             const float rem = lmax - path;
             if (rem <= s && rem <= dface) {
                 pos += mu * rem;
-                y0 = (pos - d_n) / lmax; y1 = mu; c = 2; ended = true;
+                y0 = (pos - d_n) / sqrtf(lmax); y1 = mu; c = 2; ended = true;
             } else if (dface <= s) {
                 path += dface;
                 y0 = logf(std::max(path, 1e-30f) / lmax); y1 = fabsf(mu); c = mu > 0.0f ? 1 : 0; ended = true;
@@ -1117,9 +1117,10 @@ int orc_surr_walk(uint64_t seed, const float *state, int64_t n, float *x, int32_
                 if (mu == 0.0f) mu = 1.0f;
             }
         }
-        if (!ended) { y0 = (pos - d_n) / lmax; y1 = mu; c = 2; }
-        x[4 * i] = d_n < lmax ? d_n / lmax : 1.0f;
-        x[4 * i + 1] = d_f < lmax ? d_f / lmax : 1.0f;
+        if (!ended) { y0 = (pos - d_n) / sqrtf(lmax); y1 = mu; c = 2; }
+        const float r0 = log1pf(d_n / sqrtf(lmax)) * 0.41703239f, r1 = log1pf(d_f / sqrtf(lmax)) * 0.41703239f;
+        x[4 * i] = r0 < 1.0f ? r0 : 1.0f;
+        x[4 * i + 1] = r1 < 1.0f ? r1 : 1.0f;
         x[4 * i + 2] = state[4 * i + 2];
         x[4 * i + 3] = (log10f(lmax) - 2.0f) * 0.5f;
         cls[i] = c;

@@ -51,7 +51,8 @@ def features(state):
     """(d_n, d_f, mu', lmax) rows -> network inputs."""
     s = np.asarray(state, dtype=np.float64)
     dn, df, mu, L = s[:, 0], s[:, 1], s[:, 2], s[:, 3]
-    return np.stack([np.minimum(dn / L, 1.0), np.minimum(df / L, 1.0), mu, (np.log10(L) - 2.0) * 0.5], axis=1)
+    g = lambda d: np.minimum(np.log1p(d / np.sqrt(L)) / np.log(11.0), 1.0)
+    return np.stack([g(dn), g(df), mu, (np.log10(L) - 2.0) * 0.5], axis=1)
 
 
 def forward(P, x):

@@ -40,3 +40,11 @@ def gpu_lib():
     mpimc._build.build()
     import mpimc._lib
     return mpimc._lib.load()
+
+
+@pytest.fixture(scope="session")
+def surrogate_params(gpu_lib):
+    """The learned surrogate, trained once per session on the GPU with the
+    default configuration (mpimc.surrogate.DEFAULT_TRAIN), and its loss curve."""
+    from mpimc import surrogate
+    return surrogate.train(return_loss=True)

@@ -1,0 +1,93 @@
+"""GPU tests of transport with the learned thick-cell surrogate: exact
+fallback to the analog path, reproducibility, temperatures against the analog
+ensemble on the thick-slab deck, and the work it saves there."""
+import numpy as np
+import pytest
+
+from conftest import load_deck
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(deck, seed, params=None, **ov):
+    import mpimc
+    inputs, mesh = load_deck(deck, SEED=str(seed), **ov)
+    e = mpimc.Engine(inputs, mesh)
+    if params is not None:
+        e.set_surrogate(params)
+    steps, _ = e.run()
+    out = dict(temp=e.field("temp"), rad=e.field("radenergydens"), steps=steps,
+               segments=sum(s["segments"] for s in steps), calls=sum(s["surrogate_calls"] for s in steps))
+    e.close()
+    return out
+
+
+def test_surrogate_needs_1d_and_fp32_or_fp16(surrogate_params):
+    import mpimc
+    P, _ = surrogate_params
+    for deck, ov in (("tiny_2d", {"precision": 1}), ("thick_slab", {"precision": 0, "scale_select_precision": 0})):
+        inputs, mesh = load_deck(deck)
+        e = mpimc.Engine(inputs, mesh, ov)
+        with pytest.raises(mpimc.ImcError):
+            e.set_surrogate(P)
+        assert not e.surrogate_active()
+        e.close()
+    inputs, mesh = load_deck("thick_slab")
+    e = mpimc.Engine(inputs, mesh)
+    with pytest.raises(mpimc.ImcError):
+        e.set_surrogate(P[:100])
+    e.set_surrogate(P)
+    assert e.surrogate_active()
+    e.set_surrogate(None)
+    assert not e.surrogate_active()
+    e.close()
+
+
+def test_surrogate_off_is_the_analog_path(surrogate_params):
+    """Turning the surrogate on and off again leaves the analog kernels,
+    bit for bit."""
+    import mpimc
+    P, _ = surrogate_params
+    a = _run("thick_slab", 11, NINPUT="20000", NMAX="200000")
+    inputs, mesh = load_deck("thick_slab", SEED="11", NINPUT="20000", NMAX="200000")
+    e = mpimc.Engine(inputs, mesh)
+    e.set_surrogate(P)
+    e.set_surrogate(None)
+    e.run()
+    assert np.array_equal(e.field("temp"), a["temp"])
+    e.close()
+
+
+def test_surrogate_transport_is_reproducible(surrogate_params):
+    P, _ = surrogate_params
+    a = _run("thick_slab", 12, P, NINPUT="20000", NMAX="200000")
+    b = _run("thick_slab", 12, P, NINPUT="20000", NMAX="200000")
+    assert a["calls"] > 0
+    assert np.array_equal(a["temp"], b["temp"]) and np.array_equal(a["rad"], b["rad"])
+    assert a["segments"] == b["segments"] and a["calls"] == b["calls"]
+    for s in a["steps"][:-1]:
+        assert abs(s["energy_error"]) < 1e-5 and s["error_flags"] == 0
+
+
+def test_surrogate_gain_on_thick_slab(surrogate_params):
+    """Thick slab (40 mean free paths per cell, ~400 collisions per history
+    per step): with the surrogate the analog segments fall at least 2-fold,
+    and the ensemble-mean temperature agrees with the analog ensemble --
+    per cell within 4 sigma, within 3 sigma on average (rms z < 1.6), and
+    within 0.3 % over the source region."""
+    P, _ = surrogate_params
+    A = [_run("thick_slab", 700 + i) for i in range(8)]
+    S = [_run("thick_slab", 800 + i, P) for i in range(8)]
+    seg_a = np.mean([r["segments"] for r in A])
+    seg_s = np.mean([r["segments"] for r in S])
+    assert seg_a / seg_s > 2.0, (seg_a, seg_s)
+    assert np.mean([r["calls"] for r in S]) > 1e6
+    Ta = np.array([r["temp"] for r in A])
+    Ts = np.array([r["temp"] for r in S])
+    live = Ta.mean(0) > 0.02
+    se = np.sqrt(Ta.var(0, ddof=1) / len(Ta) + Ts.var(0, ddof=1) / len(Ts))[live]
+    z = (Ts.mean(0) - Ta.mean(0))[live] / se
+    assert np.all(np.abs(z) < 4.0), np.round(z, 1)
+    assert np.sqrt(np.mean(z ** 2)) < 1.6, np.round(z, 1)
+    src = slice(0, 10)  # RADSOURCE on [0, 0.5]: cells 0-9
+    assert abs(Ts.mean(0)[src].mean() / Ta.mean(0)[src].mean() - 1.0) < 3e-3

@@ -67,7 +67,7 @@ def test_walk_without_reachable_faces_is_a_free_random_walk():
     st = np.tile([1e6, 1e6, 0.5, L], (n, 1))
     _, c, t = oracle.surr_walk(7, st)
     assert np.all(c == S.TRUNC)
-    disp = t[:, 0].astype(np.float64) * L
+    disp = t[:, 0].astype(np.float64) * np.sqrt(L)
     var = disp.var()
     assert abs(var / (2.0 * L / 3.0) - 1.0) < 0.05, var
     assert abs(disp.mean() - 0.5) < 4.0 * np.sqrt(var / n)
