@@ -27,27 +27,21 @@ namespace imc {
 template <class St, int BLOCK, bool SMT>
 __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc, PBufPair bufs) {
     typedef typename St::T T;
+    typedef SegMath<T> M;
     PBuf<St> pb(bufs.b[sc->cur]);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Tab1<T> *tab = reinterpret_cast<Tab1<T> *>(smem_raw);
     const int N = ca.nx;
     const T ds = (T)ca.ds, c = (T)ca.c;
     const bool ds_one = ds == (T)1;
+    const T rdsc = (T)1 / (ds * c);
     long long *dep_acc = ca.dep_acc, *rad_acc = ca.rad_acc;
     if (SMT) {
         dep_acc = tally_smem(smem_raw, table_bytes(ca, sizeof(T)));
         rad_acc = dep_acc + 3 * (size_t)ca.K * ca.nc;
         for (int i = threadIdx.x; i < 6 * ca.K * ca.nc; i += blockDim.x) dep_acc[i] = 0;
     }
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        T sa = (T)ca.sa[i], f = (T)ca.fleck[i], ss = (T)ca.ss[i];
-        Tab1<T> e;
-        e.saf = sa * f;
-        e.seff = sa * ((T)1 - f) + ss;
-        e.dxT = (T)ca.dx[i];
-        e.dxs = e.dxT * ds;
-        tab[i] = e;
-    }
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tab[i] = make_tab1<T>(ca.sa[i], ca.fleck[i], ca.ss[i], ca.dx[i], ds);
     __syncthreads();
     const T endsteptime = (T)sc->dt;
     const long long n = sc->n_particles;
@@ -66,8 +60,8 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         const int cs = pb.cs[i];
         int cell = cs & 0xFFFFFF;
         const int k = cs >> 24;
-        T t, x, mu, E, E0;
-        E0 = (T)pb.E0[i];
+        T t, x, mu, E;
+        const T E0 = (T)pb.E0[i];
         if (St::half) {
             t = ld_f(pb.t + i) * (float)endsteptime;
             x = ld_f(pb.x + i) * (float)tab[cell].dxs;
@@ -81,90 +75,101 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         const T minenergy = (T)(0.01 * (double)E0);
         T acc_s = (T)0, acc_c = (T)0;
         int acc_cell = cell;
-        bool alive = true;
         long long seg = 0;
-        while (true) {
-            if (++seg > cap) { flags |= (1u << 2); alive = false; break; }
-            const Tab1<T> ce = tab[cell];
-            T dist_b = mu > (T)0 ? (ce.dxs - x) / mu : m_abs(x / mu);
-            T dist_col = Rand<T>::exp1(rs) / ce.seff;
-            T dist_cen = c * (endsteptime - t) * ds;
-            T dist = jmin(jmin(dist_b, dist_col), dist_cen);
-            if (dist != dist) { flags |= 1u; alive = false; break; }
-            T newenergy = E * m_exp(-ce.saf * dist);
-            if (cell != acc_cell) {
-                flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
-                acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
-            }
-            if (newenergy <= minenergy) {
-                nadd(acc_s, acc_c, E / ce.dxT);
-                alive = false;
-                break;
-            }
-            nadd(acc_s, acc_c, -(E / ce.dxT) * m_expm1(-ce.saf * dist));
-            x += mu * dist;
-            t += (ds_one ? dist : dist / ds) / c;
-            E = newenergy;
-            if (dist == dist_b) {
-                if (mu > (T)0) {
-                    if (cell == N - 1) {
-                        if (reflect_r) {
-                            mu = -mu;
-                        } else {
-                            flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
-                            alive = false;
-                            break;
-                        }
-                    }
-                    cell += 1;
-                    x = (T)0;
-                }
-                if (mu < (T)0) {
-                    if (cell == 0) {
-                        if (reflect_l) {
-                            mu = -mu;
-                        } else {
-                            flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
-                            alive = false;
-                            break;
-                        }
-                    } else {
-                        cell -= 1;
-                        x = tab[cell].dxs;
-                    }
-                }
-            }
-            if (dist == dist_col) {
-                // mu = 1 - 2*rand, redrawn while zero (src/imc_transport.jl:178-181);
-                // a zero needs rand == 0.5 exactly, so 64 redraws never run out
-                mu = (T)0;
-                for (int r = 0; r < 64 && mu == (T)0; ++r) mu = (T)1 - (T)2 * Rand<T>::u(rs);
-                if (mu == (T)0) mu = (T)1;
-            }
-            if (dist == dist_cen) {
-                // census: t = 0, write the state back (src/imc_transport.jl:185-193)
-                T Est = E;
-                if (St::half) {
-                    st_v(pb.t + i, 0.0f);
-                    st_v(pb.x + i, (float)x / (float)tab[cell].dxs);
-                    st_v(pb.ux + i, (float)mu);
-                    __half ef = __float2half_rn((float)E / (float)E0);
-                    pb.E[i] = ef;
-                    Est = __half2float(ef) * (float)E0;
+        int end = 0;  // 1 killed / escaped, 2 census
+        while (!end) {
+            // one pass of the reference's while loop (src/imc_transport.jl:73-195)
+            if (++seg > cap) {
+                flags |= (1u << 2);
+                end = 1;
+            } else {
+                const Tab1<T> ce = tab[cell];
+                const T dist_b = mu > (T)0 ? (ce.dxs - x) / mu : m_abs(x / mu);
+                const T dist_col = M::flight(rs, ce);
+                const T dist_cen = c * (endsteptime - t) * ds;
+                const T dist = jmin(jmin(dist_b, dist_col), dist_cen);
+                if (dist != dist) {
+                    flags |= 1u;
+                    end = 1;
                 } else {
-                    pb.t[i] = (typename St::S)0;
-                    pb.x[i] = (typename St::S)x;
-                    pb.ux[i] = (typename St::S)mu;
-                    pb.E[i] = (typename St::S)E;
+                    T dep;
+                    const T newenergy = M::attenuate(E, ce, dist, &dep);
+                    if (cell != acc_cell) {
+                        flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+                        acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
+                    }
+                    if (newenergy <= minenergy) {
+                        nadd(acc_s, acc_c, M::all_in(E, ce));
+                        end = 1;
+                    } else {
+                        nadd(acc_s, acc_c, dep);
+                        x += mu * dist;
+                        if constexpr (sizeof(T) == 4) t += dist * rdsc;
+                        else t += (ds_one ? dist : dist / ds) / c;
+                        E = newenergy;
+                        if (dist == dist_b) {
+                            if (mu > (T)0) {
+                                if (cell == N - 1) {
+                                    if (reflect_r) {
+                                        mu = -mu;
+                                    } else {
+                                        flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
+                                        end = 1;
+                                    }
+                                }
+                                if (!end) {
+                                    cell += 1;
+                                    x = (T)0;
+                                }
+                            }
+                            if (!end && mu < (T)0) {
+                                if (cell == 0) {
+                                    if (reflect_l) {
+                                        mu = -mu;
+                                    } else {
+                                        flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
+                                        end = 1;
+                                    }
+                                } else {
+                                    cell -= 1;
+                                    x = tab[cell].dxs;
+                                }
+                            }
+                        }
+                        if (!end && dist == dist_col) {
+                            // mu = 1 - 2*rand, redrawn while zero (src/imc_transport.jl:178-181);
+                            // a zero needs rand == 0.5 exactly, so 64 redraws never run out
+                            mu = (T)0;
+                            for (int r = 0; r < 64 && mu == (T)0; ++r) mu = (T)1 - (T)2 * Rand<T>::u(rs);
+                            if (mu == (T)0) mu = (T)1;
+                        }
+                        if (!end && dist == dist_cen) {
+                            // census: t = 0, write the state back (src/imc_transport.jl:185-193)
+                            T Est = E;
+                            if (St::half) {
+                                st_v(pb.t + i, 0.0f);
+                                st_v(pb.x + i, (float)x / (float)tab[cell].dxs);
+                                st_v(pb.ux + i, (float)mu);
+                                __half ef = __float2half_rn((float)E / (float)E0);
+                                pb.E[i] = ef;
+                                Est = __half2float(ef) * (float)E0;
+                            } else {
+                                pb.t[i] = (typename St::S)0;
+                                pb.x[i] = (typename St::S)x;
+                                pb.ux[i] = (typename St::S)mu;
+                                pb.E[i] = (typename St::S)E;
+                            }
+                            if (cell != (cs & 0xFFFFFF)) pb.cs[i] = cell | (k << 24);
+                            flush_one<T, SMT>(rad_acc, k * nc + cell, Est, b_rad, flags);
+                            emax = Est > emax ? Est : emax;
+                            end = 2;
+                        }
+                    }
                 }
-                if (cell != (cs & 0xFFFFFF)) pb.cs[i] = cell | (k << 24);
-                flush_one<T, SMT>(rad_acc, k * nc + cell, Est, b_rad, flags);
-                emax = Est > emax ? Est : emax;
-                break;
             }
         }
         flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
-        if (!alive) pb.alive[i] = 0;
+        if (end == 1) pb.alive[i] = 0;
         segs += (unsigned long long)seg;
     }
     if (SMT) flush_block_tallies(ca, dep_acc);
@@ -346,7 +351,8 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
 
 // Launch shape of the transport kernel.  When the table and the block's
 // private tallies fit in shared memory the kernel runs one large block per
-// SM with shared tallies (BLOCK 768 for FP32 / FP16 state, 512 for FP64);
+// SM with shared tallies (kSmtBlock32 threads for FP32 / FP16 state,
+// kSmtBlock64 for FP64);
 // otherwise 256-thread blocks with tallies in global memory.
 constexpr int kSmemBudget = 200 * 1024;
 
@@ -357,7 +363,7 @@ TransportShape transport_shape(const CellArgs &ca, int prec) {
     const long long tallies = 2ll * 3 * 8 * (long long)ca.K * ca.nc;
     sh.smem_tally = table + tallies <= kSmemBudget;
     sh.smem = sh.smem_tally ? (int)(table + tallies) : table;
-    sh.block = sh.smem_tally ? (prec == 0 ? 512 : 768) : 256;
+    sh.block = sh.smem_tally ? (prec == 0 ? kSmtBlock64 : kSmtBlock32) : 256;
     return sh;
 }
 
@@ -368,9 +374,9 @@ template <class St, int B, bool SMT> static const void *kptr(int geometry) {
 const void *transport_kernel_ptr(const CellArgs &ca, int prec) {
     TransportShape sh = transport_shape(ca, prec);
     if (sh.smem_tally) {
-        if (prec == 0) return kptr<StF64, 512, true>(ca.geometry);
-        if (prec == 1) return kptr<StF32, 768, true>(ca.geometry);
-        return kptr<StF16, 768, true>(ca.geometry);
+        if (prec == 0) return kptr<StF64, kSmtBlock64, true>(ca.geometry);
+        if (prec == 1) return kptr<StF32, kSmtBlock32, true>(ca.geometry);
+        return kptr<StF16, kSmtBlock32, true>(ca.geometry);
     }
     if (prec == 0) return kptr<StF64, 256, false>(ca.geometry);
     if (prec == 1) return kptr<StF32, 256, false>(ca.geometry);
@@ -386,9 +392,9 @@ static void launch_one(const CellArgs &ca, Scalars *sc, PBufPair buf, int grid, 
 void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufPair buf, int grid, cudaStream_t st) {
     TransportShape sh = transport_shape(ca, prec);
     if (sh.smem_tally) {
-        if (prec == 0) launch_one<StF64, 512, true>(ca, sc, buf, grid, sh.smem, st);
-        else if (prec == 1) launch_one<StF32, 768, true>(ca, sc, buf, grid, sh.smem, st);
-        else launch_one<StF16, 768, true>(ca, sc, buf, grid, sh.smem, st);
+        if (prec == 0) launch_one<StF64, kSmtBlock64, true>(ca, sc, buf, grid, sh.smem, st);
+        else if (prec == 1) launch_one<StF32, kSmtBlock32, true>(ca, sc, buf, grid, sh.smem, st);
+        else launch_one<StF16, kSmtBlock32, true>(ca, sc, buf, grid, sh.smem, st);
     } else {
         if (prec == 0) launch_one<StF64, 256, false>(ca, sc, buf, grid, sh.smem, st);
         else if (prec == 1) launch_one<StF32, 256, false>(ca, sc, buf, grid, sh.smem, st);

@@ -45,8 +45,9 @@ template <bool SMT> __device__ __forceinline__ void add_limbs(long long *a, cons
 }
 
 // bytes of the per-cell transport table at the start of dynamic shared memory
+// (1D: one 32-byte Tab1 per cell for either type)
 __host__ __device__ __forceinline__ int table_bytes(const CellArgs &ca, int tsz) {
-    int b = ca.geometry == 1 ? 4 * tsz * ca.nx : 2 * tsz * (ca.nc + ca.nx + ca.ny);
+    int b = ca.geometry == 1 ? 32 * ca.nx : 2 * tsz * (ca.nc + ca.nx + ca.ny);
     return (b + 15) & ~15;
 }
 
@@ -90,7 +91,66 @@ __device__ __forceinline__ void flush_one(long long *acc, int slot, T v, int b, 
     add_limbs<SMT>(acc + 3 * (size_t)slot, A);
 }
 
-template <class T> struct Tab1 { T saf, seff, dxs, dxT; };
+// threads per block of the shared-tally transport kernels: FP32 / FP16 state
+// and FP64 state (one block per SM: the table and the private tallies take
+// most of the shared memory)
+constexpr int kSmtBlock32 = 1024;
+constexpr int kSmtBlock64 = 512;
+
+// 1D per-cell table: sigma_a f, effective scatter, width * distancescale,
+// width; the FP32 table adds the reciprocals its arithmetic multiplies by
+template <class T> struct Tab1;
+template <> struct Tab1<double> { double saf, seff, dxs, dxT; };
+template <> struct Tab1<float> { float saf, seff, dxs, dxT, rseff, rdxT, pad0, pad1; };
+static_assert(sizeof(Tab1<double>) == 32 && sizeof(Tab1<float>) == 32, "32-byte table rows");
+
+template <class T>
+__device__ __forceinline__ Tab1<T> make_tab1(double sa, double f, double ss, double dx, T ds) {
+    Tab1<T> e;
+    const T saT = (T)sa, fT = (T)f, ssT = (T)ss;
+    e.saf = saT * fT;
+    e.seff = saT * ((T)1 - fT) + ssT;
+    e.dxT = (T)dx;
+    e.dxs = e.dxT * ds;
+    if constexpr (sizeof(T) == 4) {
+        e.rseff = 1.0f / e.seff;  // inf for a zero opacity: the flight is then inf, as seff/0 is
+        e.rdxT = 1.0f / e.dxT;
+        e.pad0 = e.pad1 = 0.0f;
+    }
+    return e;
+}
+
+// Segment arithmetic of Transport.MC (src/imc_transport.jl:84-123).  FP64
+// evaluates the reference's expressions as written.  FP32 (and FP16 state)
+// evaluates the same quantities with fewer instructions: the collision
+// distance as -log(v) * (1/seff) with the hardware logarithm, the weight
+// after the segment as E + E expm1(-sigma_a f d) -- one transcendental for
+// both the attenuation and the deposit, so the two add up to E up to one
+// rounding -- and reciprocals instead of divisions.
+template <class T> struct SegMath;
+template <> struct SegMath<double> {
+    static __device__ __forceinline__ double flight(Stream &rs, const Tab1<double> &ce) {
+        return Rand<double>::exp1(rs) / ce.seff;
+    }
+    // new weight; *dep = the deposit per unit width
+    static __device__ __forceinline__ double attenuate(double E, const Tab1<double> &ce, double d, double *dep) {
+        *dep = -(E / ce.dxT) * expm1(-ce.saf * d);
+        return E * exp(-ce.saf * d);
+    }
+    static __device__ __forceinline__ double all_in(double E, const Tab1<double> &ce) { return E / ce.dxT; }
+};
+template <> struct SegMath<float> {
+    static __device__ __forceinline__ float flight(Stream &rs, const Tab1<float> &ce) {
+        const float v = (float)((rs.next() >> 8) | 1u) * 0x1p-24f;
+        return -__logf(v) * ce.rseff;
+    }
+    static __device__ __forceinline__ float attenuate(float E, const Tab1<float> &ce, float d, float *dep) {
+        const float em1 = expm1f(-ce.saf * d);
+        *dep = -(E * ce.rdxT) * em1;
+        return E + E * em1;
+    }
+    static __device__ __forceinline__ float all_in(float E, const Tab1<float> &ce) { return E * ce.rdxT; }
+};
 template <class T> struct Tab2 { T saf, seff; };
 template <class T> struct Face { T ws, wT; };  // width * distancescale, width
 

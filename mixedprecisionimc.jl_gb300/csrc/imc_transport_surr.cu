@@ -163,17 +163,18 @@ __device__ __forceinline__ int analog_segment(const CellArgs &ca, const Tab1<T> 
     if (++h.seg > cap) { flags |= (1u << 2); return kKilled; }
     const Tab1<T> ce = tab[h.cell];
     const T dist_b = h.mu > (T)0 ? (ce.dxs - h.x) / h.mu : m_abs(h.x / h.mu);
-    const T dist_col = Rand<T>::exp1(h.rs) / ce.seff;
+    const T dist_col = SegMath<T>::flight(h.rs, ce);
     const T dist_cen = c * (dt - h.t) * ds;
     const T dist = jmin(jmin(dist_b, dist_col), dist_cen);
     if (dist != dist) { flags |= 1u; return kKilled; }
-    const T newenergy = h.E * m_exp(-ce.saf * dist);
+    T dep;
+    const T newenergy = SegMath<T>::attenuate(h.E, ce, dist, &dep);
     follow_cell<T, SMT>(h, dep_acc, nc, b_dep, flags);
     if (newenergy <= h.minenergy) {
-        nadd(h.acc_s, h.acc_c, h.E / ce.dxT);
+        nadd(h.acc_s, h.acc_c, SegMath<T>::all_in(h.E, ce));
         return kKilled;
     }
-    nadd(h.acc_s, h.acc_c, -(h.E / ce.dxT) * m_expm1(-ce.saf * dist));
+    nadd(h.acc_s, h.acc_c, dep);
     h.x += h.mu * dist;
     h.t += (ds_one ? dist : dist / ds) / c;
     h.E = newenergy;
@@ -229,7 +230,7 @@ __device__ __forceinline__ int apply_outcome(const CellArgs &ca, const Tab1<T> *
     if (++h.seg > cap) { flags |= (1u << 2); return kKilled; }
     const Tab1<T> ce = tab[h.cell];
     if (cls == kTrunc && q.cut) {
-        nadd(h.acc_s, h.acc_c, h.E / ce.dxT);
+        nadd(h.acc_s, h.acc_c, SegMath<T>::all_in(h.E, ce));
         return kKilled;
     }
     const float seff = (float)ce.seff;
@@ -254,12 +255,13 @@ __device__ __forceinline__ int apply_outcome(const CellArgs &ca, const Tab1<T> *
         dist = (T)(l / seff);
         face = true;
     }
-    const T newenergy = h.E * m_exp(-ce.saf * dist);
+    T dep;
+    const T newenergy = SegMath<T>::attenuate(h.E, ce, dist, &dep);
     if (newenergy <= h.minenergy) {
-        nadd(h.acc_s, h.acc_c, h.E / ce.dxT);
+        nadd(h.acc_s, h.acc_c, SegMath<T>::all_in(h.E, ce));
         return kKilled;
     }
-    nadd(h.acc_s, h.acc_c, -(h.E / ce.dxT) * m_expm1(-ce.saf * dist));
+    nadd(h.acc_s, h.acc_c, dep);
     h.t += (ds_one ? dist : dist / ds) / c;
     if (h.t > dt) h.t = dt;
     h.E = newenergy;
@@ -306,15 +308,7 @@ __device__ __forceinline__ void load_queued(const SurrQueue &qq, long long e, un
 
 template <class T>
 __device__ __forceinline__ void fill_table(const CellArgs &ca, Tab1<T> *tab, T ds) {
-    for (int i = threadIdx.x; i < ca.nx; i += blockDim.x) {
-        T sa = (T)ca.sa[i], f = (T)ca.fleck[i], ss = (T)ca.ss[i];
-        Tab1<T> e;
-        e.saf = sa * f;
-        e.seff = sa * ((T)1 - f) + ss;
-        e.dxT = (T)ca.dx[i];
-        e.dxs = e.dxT * ds;
-        tab[i] = e;
-    }
+    for (int i = threadIdx.x; i < ca.nx; i += blockDim.x) tab[i] = make_tab1<T>(ca.sa[i], ca.fleck[i], ca.ss[i], ca.dx[i], ds);
 }
 
 // Per-cell gate of the analog passes: 0 where no history can want a query
@@ -351,7 +345,7 @@ __device__ __forceinline__ int walk_analog(const CellArgs &ca, const Tab1<T> *ta
                 const int kind = decide<T>(ce, h, c, ds, dt, q);
                 if (kind == kCertainKill) {
                     follow_cell<T, SMT>(h, dep_acc, nc, b_dep, flags);
-                    nadd(h.acc_s, h.acc_c, h.E / ce.dxT);
+                    nadd(h.acc_s, h.acc_c, SegMath<T>::all_in(h.E, ce));
                     h.seg += 1;
                     calls += 1;
                     res = kKilled;
@@ -509,7 +503,7 @@ __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scal
                                        b_lost, flags);
                 calls += 1;
             } else if (kind == kCertainKill) {
-                nadd(h.acc_s, h.acc_c, h.E / tab[h.cell].dxT);
+                nadd(h.acc_s, h.acc_c, SegMath<T>::all_in(h.E, tab[h.cell]));
                 calls += 1;
                 res = kKilled;
             }
@@ -580,17 +574,17 @@ SurrShapes surr_shapes(const CellArgs &ca, int prec) {
 const void *surr_kernel_ptr(const CellArgs &ca, int prec, int which) {
     const bool smt = transport_shape(ca, prec).smem_tally;
     if (which == 3) return prec == 2 ? (const void *)k_wave_query<StF16> : (const void *)k_wave_query<StF32>;
-    if (prec == 2) return smt ? analog_ptr<StF16, 768, true>(which) : analog_ptr<StF16, 256, false>(which);
-    return smt ? analog_ptr<StF32, 768, true>(which) : analog_ptr<StF32, 256, false>(which);
+    if (prec == 2) return smt ? analog_ptr<StF16, kSmtBlock32, true>(which) : analog_ptr<StF16, 256, false>(which);
+    return smt ? analog_ptr<StF32, kSmtBlock32, true>(which) : analog_ptr<StF32, 256, false>(which);
 }
 
 void launch_transport_surr(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, const SurrWave &w,
                            const SurrShapes &sh, cudaStream_t st) {
     if (prec == 2) {
-        if (sh.analog_smt) launch_wave<StF16, 768, true>(ca, sc, bufs, w, sh, st);
+        if (sh.analog_smt) launch_wave<StF16, kSmtBlock32, true>(ca, sc, bufs, w, sh, st);
         else launch_wave<StF16, 256, false>(ca, sc, bufs, w, sh, st);
     } else {
-        if (sh.analog_smt) launch_wave<StF32, 768, true>(ca, sc, bufs, w, sh, st);
+        if (sh.analog_smt) launch_wave<StF32, kSmtBlock32, true>(ca, sc, bufs, w, sh, st);
         else launch_wave<StF32, 256, false>(ca, sc, bufs, w, sh, st);
     }
 }

@@ -179,6 +179,12 @@ def main(args, verbose=True, saved=False):
     mesh = Mesh.mesh_generation(inputs)
     simvars = make_simvars(inputs, mesh)
     eng = ensure_engine(inputs, mesh)
+    if str(inputs.get("RANDOMWALK", "FALSE")).upper() == "TRUE":
+        # src/MixedPrecisionIMC.jl:127,140: Transport.MC_RW -> the learned surrogate
+        from . import surrogate
+        on = surrogate.enable(eng)
+        if verbose:
+            print("Random walk: learned thick-cell surrogate", "on" if on else "off (needs 1D, FP32/FP16 state)")
     res = RunResult(inputs=inputs, mesh=mesh, simvars=simvars)
     ts = str(inputs["TIMESTEPPING"]).upper()
     if saved:

@@ -57,6 +57,27 @@ def train(seed=None, n_samples=None, batch=None, iterations=None, lr=None, lr_mi
     return (P, loss) if return_loss else P
 
 
+_CACHE = {}
+
+
+def trained_params():
+    """The default network, trained once per process (about 2.5 s on a GB300)."""
+    if "P" not in _CACHE:
+        _CACHE["P"] = train()
+    return _CACHE["P"]
+
+
+def enable(engine):
+    """Turns the surrogate on for an Engine if its deck allows it (1D, FP32 or
+    FP16 particle state); returns whether it is on."""
+    if engine.surrogate_active():
+        return True
+    if engine.geometry != _lib.IMC_GEOM_1D or engine.deck.precision == _lib.IMC_FP64:
+        return False
+    engine.set_surrogate(trained_params())
+    return True
+
+
 def walk(seed, state=None, n=None):
     """Analog in-cell walks: (x n x 4, cls n, tgt n x 2).  state: n x 4 rows of
     (d_n, d_f, mu', lmax), or None to draw n training states."""

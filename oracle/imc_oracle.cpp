@@ -36,6 +36,13 @@
  *     sequential or pairwise `sum`; they differ only by rounding.
  *   - A history whose distance turns NaN is killed and flagged instead of
  *     looping; a history stops at a segment cap and is flagged.
+ *   - FP32 particle arithmetic in 1D transport takes the kernels' shorter
+ *     formulation of the same quantities: collision distance -log(v)/seff as
+ *     -log(v) * (1/seff), the weight after a segment E exp(-a) as
+ *     E + E expm1(-a) (the deposit uses the same expm1, so attenuation and
+ *     deposit add up to E), and reciprocals of dx and ds*c instead of
+ *     divisions.  They differ from the reference's FP32 evaluation by
+ *     roundings only; FP64 keeps the reference's expressions.
  */
 #include "../include/imc.h"
 #include "philox.h"
@@ -446,14 +453,22 @@ void transport_1d(Sim &s) {
     const int N = s.nx;
     const T endsteptime = (T)s.dt, c = (T)s.d.phys_c, ds = (T)s.d.distancescale;
     const int64_t cap = s.d.segment_cap > 0 ? s.d.segment_cap : 10000000;
-    std::vector<T> saf(N), seff(N), dxs(N), dxT(N);
+    std::vector<T> saf(N), seff(N), dxs(N), dxT(N), rseff(N), rdxT(N);
     for (int i = 0; i < N; ++i) {
         T sa = (T)s.sa[i], f = (T)s.fleck[i], ss = (T)s.ss[i];
         saf[i] = sa * f;
         seff[i] = sa * ((T)1 - f) + ss;
         dxT[i] = (T)s.dx[i];
         dxs[i] = dxT[i] * ds;
+        rseff[i] = (T)1 / seff[i];
+        rdxT[i] = (T)1 / dxT[i];
     }
+    // FP32 evaluates the segment with the kernels' formulation: collision
+    // distance -log(v) * (1/seff), weight E + E expm1(-sigma_a f d) (one
+    // transcendental for attenuation and deposit), reciprocals for divisions.
+    // FP64 evaluates the reference's expressions as written.
+    constexpr bool kF32 = sizeof(T) == 4;
+    const T rdsc = (T)1 / (ds * c);
     for (size_t pi = 0; pi < s.parts.size(); ++pi) {
         OP &p = s.parts[pi];
         if (!p.alive) continue;
@@ -477,19 +492,28 @@ void transport_1d(Sim &s) {
             ++s.segments;
             if (++seg > cap) { s.flags |= IMC_FLAG_SEGMENT_CAP; p.alive = false; break; }
             T dist_b = mu > (T)0 ? (dxs[cell] - position) / mu : std::fabs(position / mu);
-            T dist_col = RandT<T>::randexp(&rs) / seff[cell];
+            T dist_col = kF32 ? RandT<T>::randexp(&rs) * rseff[cell] : RandT<T>::randexp(&rs) / seff[cell];
             T dist_cen = c * (endsteptime - currenttime) * ds;
             T dist = jmin(jmin(dist_b, dist_col), dist_cen);
             if (dist != dist) { s.flags |= IMC_FLAG_NAN; p.alive = false; break; }
-            T newenergy = energy * std::exp(-saf[cell] * dist);
+            T newenergy, dep;
+            if (kF32) {
+                const T em1 = std::expm1(-saf[cell] * dist);
+                newenergy = energy + energy * em1;
+                dep = -(energy * rdxT[cell]) * em1;
+            } else {
+                newenergy = energy * std::exp(-saf[cell] * dist);
+                dep = -(energy / dxT[cell]) * std::expm1(-saf[cell] * dist);
+            }
             if (newenergy <= minenergy) {
-                dep_add(s, k, cell, (double)(energy / dxT[cell]));
+                dep_add(s, k, cell, (double)(kF32 ? energy * rdxT[cell] : energy / dxT[cell]));
                 p.alive = false;
                 break;
             }
-            dep_add(s, k, cell, (double)(-(energy / dxT[cell]) * std::expm1(-saf[cell] * dist)));
+            dep_add(s, k, cell, (double)dep);
             position += mu * dist;
-            currenttime += (dist / ds) / c;
+            if (kF32) currenttime += dist * rdsc;
+            else currenttime += (dist / ds) / c;
             energy = newenergy;
             if (dist == dist_b) {
                 if (mu > (T)0) {

@@ -91,3 +91,22 @@ def test_surrogate_gain_on_thick_slab(surrogate_params):
     assert np.sqrt(np.mean(z ** 2)) < 1.6, np.round(z, 1)
     src = slice(0, 10)  # RADSOURCE on [0, 0.5]: cells 0-9
     assert abs(Ts.mean(0)[src].mean() / Ta.mean(0)[src].mean() - 1.0) < 3e-3
+
+
+def test_main_with_randomwalk_uses_the_surrogate(tmp_path, surrogate_params):
+    """RANDOMWALK = TRUE (src/MixedPrecisionIMC.jl:127,140: Transport.MC_RW)
+    runs main(args) with the learned surrogate."""
+    import os
+    import mpimc
+    from mpimc import surrogate
+    from conftest import deck_path
+    surrogate._CACHE["P"] = surrogate_params[0]
+    text = open(deck_path("thick_slab")).read()
+    text = text.replace("RANDOMWALK = FALSE", "RANDOMWALK = TRUE").replace("NINPUT = 200000", "NINPUT = 20000")
+    text = text.replace("NMAX = 2000000", "NMAX = 200000")
+    p = os.path.join(str(tmp_path), "thick_rw.txt")
+    open(p, "w").write(text)
+    res = mpimc.main([p], verbose=False)
+    assert sum(s["surrogate_calls"] for s in res.steps) > 0
+    plain = mpimc.main([deck_path("thick_slab")], verbose=False)
+    assert sum(s["surrogate_calls"] for s in plain.steps) == 0
