@@ -77,6 +77,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         int acc_cell = cell;
         long long seg = 0;
         int end = 0;  // 1 killed / escaped, 2 census
+        T rmu = (T)1 / mu;  // FP32: the face distance as a product (reset at each new direction)
         while (!end) {
             // one pass of the reference's while loop (src/imc_transport.jl:73-195)
             if (++seg > cap) {
@@ -84,7 +85,9 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
                 end = 1;
             } else {
                 const Tab1<T> ce = tab[cell];
-                const T dist_b = mu > (T)0 ? (ce.dxs - x) / mu : m_abs(x / mu);
+                T dist_b;
+                if constexpr (sizeof(T) == 4) dist_b = mu > (T)0 ? (ce.dxs - x) * rmu : m_abs(x * rmu);
+                else dist_b = mu > (T)0 ? (ce.dxs - x) / mu : m_abs(x / mu);
                 const T dist_col = M::flight(rs, ce);
                 const T dist_cen = c * (endsteptime - t) * ds;
                 const T dist = jmin(jmin(dist_b, dist_col), dist_cen);
@@ -112,6 +115,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
                                 if (cell == N - 1) {
                                     if (reflect_r) {
                                         mu = -mu;
+                                        rmu = -rmu;
                                     } else {
                                         flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
                                         end = 1;
@@ -126,6 +130,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
                                 if (cell == 0) {
                                     if (reflect_l) {
                                         mu = -mu;
+                                        rmu = -rmu;
                                     } else {
                                         flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
                                         end = 1;
@@ -142,6 +147,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
                             mu = (T)0;
                             for (int r = 0; r < 64 && mu == (T)0; ++r) mu = (T)1 - (T)2 * Rand<T>::u(rs);
                             if (mu == (T)0) mu = (T)1;
+                            rmu = (T)1 / mu;
                         }
                         if (!end && dist == dist_cen) {
                             // census: t = 0, write the state back (src/imc_transport.jl:185-193)
@@ -187,6 +193,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
     Face<T> *fy = fx + NX;
     const T ds = (T)ca.ds, c = (T)ca.c;
     const bool ds_one = ds == (T)1;
+    const T rdsc = (T)1 / (ds * c);
     long long *dep_acc = ca.dep_acc, *rad_acc = ca.rad_acc;
     if (SMT) {
         dep_acc = tally_smem(smem_raw, table_bytes(ca, sizeof(T)));
@@ -198,6 +205,10 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
         Tab2<T> e;
         e.saf = sa * f;
         e.seff = sa * ((T)1 - f) + ss;
+        if constexpr (sizeof(T) == 4) {
+            e.rseff = 1.0f / e.seff;
+            e.rarea = 1.0f / ((float)ca.dx[i % NX] * (float)ca.dy[i / NX]);
+        }
         tab[i] = e;
     }
     for (int i = threadIdx.x; i < NX; i += blockDim.x) { fx[i].wT = (T)ca.dx[i]; fx[i].ws = fx[i].wT * ds; }
@@ -250,25 +261,41 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
             else dist_b = jmin(dist_bx, dist_by);
             const int cell = xi + yi * NX;
             const Tab2<T> ce = tab[cell];
-            T dist_col = Rand<T>::exp1(rs) / ce.seff;
+            T dist_col, Edens, newenergy, dep;
+            if constexpr (sizeof(T) == 4) {
+                // FP32: the 1D kernels' formulation (SegMath<float>)
+                const float v = (float)((rs.next() >> 8) | 1u) * 0x1p-24f;
+                dist_col = -__logf(v) * ce.rseff;
+            } else {
+                dist_col = Rand<T>::exp1(rs) / ce.seff;
+            }
             T dist_cen = c * (dtT - t) * ds;
             T dist = jmin(jmin(dist_b, dist_col), dist_cen);
             if (dist != dist) { flags |= 1u; alive = false; break; }
-            T newenergy = E * m_exp(-ce.saf * dist);
+            if constexpr (sizeof(T) == 4) {
+                const float em1 = expm1f(-ce.saf * dist);
+                newenergy = E + E * em1;
+                Edens = E * ce.rarea;
+                dep = -Edens * em1;
+            } else {
+                newenergy = E * m_exp(-ce.saf * dist);
+                Edens = (E / fx[xi].wT) / fy[yi].wT;
+                dep = -Edens * m_expm1(-ce.saf * dist);
+            }
             if (cell != acc_cell) {
                 flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
                 acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
             }
-            const T Edens = (E / fx[xi].wT) / fy[yi].wT;
             if (newenergy <= minenergy) {
                 nadd(acc_s, acc_c, Edens);
                 alive = false;
                 break;
             }
-            nadd(acc_s, acc_c, -Edens * m_expm1(-ce.saf * dist));
+            nadd(acc_s, acc_c, dep);
             xp += dist * vx;
             yp += dist * vy;
-            t += (ds_one ? dist : dist / ds) / c;
+            if constexpr (sizeof(T) == 4) t += dist * rdsc;
+            else t += (ds_one ? dist : dist / ds) / c;
             E = newenergy;
             if (dist == dist_bx || dist == dist_by) {
                 if (dist_bx < dist_by) {
@@ -312,8 +339,10 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
             }
             if (dist == dist_col) {
                 // isotropic re-emission: angle 2*pi*rand in Float64, rounded to T
+                // (FP32: the hardware sine and cosine)
                 T ang = (T)(6.283185307179586 * (double)Rand<T>::u(rs));
-                m_sincos(ang, &vy, &vx);
+                if constexpr (sizeof(T) == 4) __sincosf(ang, &vy, &vx);
+                else m_sincos(ang, &vy, &vx);
             }
             if (dist == dist_cen) {
                 const int cellf = xi + yi * NX;

@@ -47,7 +47,8 @@ template <bool SMT> __device__ __forceinline__ void add_limbs(long long *a, cons
 // bytes of the per-cell transport table at the start of dynamic shared memory
 // (1D: one 32-byte Tab1 per cell for either type)
 __host__ __device__ __forceinline__ int table_bytes(const CellArgs &ca, int tsz) {
-    int b = ca.geometry == 1 ? 32 * ca.nx : 2 * tsz * (ca.nc + ca.nx + ca.ny);
+    // 1D: 32-byte Tab1 rows; 2D: 16-byte Tab2 rows, then x and y Face rows
+    int b = ca.geometry == 1 ? 32 * ca.nx : 16 * ca.nc + 2 * tsz * (ca.nx + ca.ny);
     return (b + 15) & ~15;
 }
 
@@ -151,7 +152,12 @@ template <> struct SegMath<float> {
     }
     static __device__ __forceinline__ float all_in(float E, const Tab1<float> &ce) { return E * ce.rdxT; }
 };
-template <class T> struct Tab2 { T saf, seff; };
+// 2D per-cell table: sigma_a f, effective scatter; FP32 adds 1/seff and the
+// reciprocal cell area
+template <class T> struct Tab2;
+template <> struct Tab2<double> { double saf, seff; };
+template <> struct Tab2<float> { float saf, seff, rseff, rarea; };
+static_assert(sizeof(Tab2<double>) == 16 && sizeof(Tab2<float>) == 16, "16-byte table rows");
 template <class T> struct Face { T ws, wT; };  // width * distancescale, width
 
 // end-of-kernel reduction of per-thread counters: one atomic per warp

@@ -36,12 +36,13 @@
  *     sequential or pairwise `sum`; they differ only by rounding.
  *   - A history whose distance turns NaN is killed and flagged instead of
  *     looping; a history stops at a segment cap and is flagged.
- *   - FP32 particle arithmetic in 1D transport takes the kernels' shorter
+ *   - FP32 particle arithmetic in 1D and 2D transport takes the kernels' shorter
  *     formulation of the same quantities: collision distance -log(v)/seff as
  *     -log(v) * (1/seff), the weight after a segment E exp(-a) as
  *     E + E expm1(-a) (the deposit uses the same expm1, so attenuation and
  *     deposit add up to E), and reciprocals of dx and ds*c instead of
- *     divisions.  They differ from the reference's FP32 evaluation by
+ *     divisions (also 1/mu, set at each new direction, for the face
+ *     distance).  They differ from the reference's FP32 evaluation by
  *     roundings only; FP64 keeps the reference's expressions.
  */
 #include "../include/imc.h"
@@ -488,10 +489,12 @@ void transport_1d(Sim &s) {
         }
         const T minenergy = (T)(0.01 * (double)startenergy);
         int64_t seg = 0;
+        T rmu = (T)1 / mu;
         while (true) {
             ++s.segments;
             if (++seg > cap) { s.flags |= IMC_FLAG_SEGMENT_CAP; p.alive = false; break; }
-            T dist_b = mu > (T)0 ? (dxs[cell] - position) / mu : std::fabs(position / mu);
+            T dist_b = kF32 ? (mu > (T)0 ? (dxs[cell] - position) * rmu : std::fabs(position * rmu))
+                            : (mu > (T)0 ? (dxs[cell] - position) / mu : std::fabs(position / mu));
             T dist_col = kF32 ? RandT<T>::randexp(&rs) * rseff[cell] : RandT<T>::randexp(&rs) / seff[cell];
             T dist_cen = c * (endsteptime - currenttime) * ds;
             T dist = jmin(jmin(dist_b, dist_col), dist_cen);
@@ -520,6 +523,7 @@ void transport_1d(Sim &s) {
                     if (cell == N - 1) {
                         if (s.d.bc[IMC_RIGHT] == IMC_BC_REFLECT) {
                             mu = -mu;
+                            rmu = -rmu;
                         } else {
                             s.lost_k[k].add((double)energy);
                             p.alive = false;
@@ -533,6 +537,7 @@ void transport_1d(Sim &s) {
                     if (cell == 0) {
                         if (s.d.bc[IMC_LEFT] == IMC_BC_REFLECT) {
                             mu = -mu;
+                            rmu = -rmu;
                         } else {
                             s.lost_k[k].add((double)energy);
                             p.alive = false;
@@ -548,6 +553,7 @@ void transport_1d(Sim &s) {
                 mu = (T)0;
                 for (int r = 0; r < 64 && mu == (T)0; ++r) mu = (T)1 - (T)2 * RandT<T>::rand(&rs);
                 if (mu == (T)0) mu = (T)1;
+                rmu = (T)1 / mu;
             }
             if (dist == dist_cen) {
                 p.cell = cell;
@@ -573,12 +579,17 @@ void transport_2d(Sim &s) {
     const int NX = s.nx, NY = s.ny;
     const T c = (T)s.d.phys_c, ds = (T)s.d.distancescale, dtT = (T)s.dt;
     const int64_t cap = s.d.segment_cap > 0 ? s.d.segment_cap : 10000000;
-    std::vector<T> saf(s.nc), seff(s.nc), dxT(NX), dyT(NY), dxs(NX), dys(NY);
+    std::vector<T> saf(s.nc), seff(s.nc), rseff(s.nc), rarea(s.nc), dxT(NX), dyT(NY), dxs(NX), dys(NY);
     for (int i = 0; i < s.nc; ++i) {
         T sa = (T)s.sa[i], f = (T)s.fleck[i], ss = (T)s.ss[i];
         saf[i] = sa * f;
         seff[i] = sa * ((T)1 - f) + ss;
+        rseff[i] = (T)1 / seff[i];
+        rarea[i] = (T)1 / ((T)s.dx[i % NX] * (T)s.dy[i / NX]);
     }
+    // FP32: the kernels' shorter formulation (as in transport_1d)
+    constexpr bool kF32 = sizeof(T) == 4;
+    const T rdsc = (T)1 / (ds * c);
     for (int i = 0; i < NX; ++i) { dxT[i] = (T)s.dx[i]; dxs[i] = dxT[i] * ds; }
     for (int j = 0; j < NY; ++j) { dyT[j] = (T)s.dy[j]; dys[j] = dyT[j] * ds; }
     for (size_t pi = 0; pi < s.parts.size(); ++pi) {
@@ -611,20 +622,30 @@ void transport_2d(Sim &s) {
             else if (dist_by != dist_by) dist_b = dist_bx;
             else dist_b = jmin(dist_bx, dist_by);
             int cell = xi + yi * NX;
-            T dist_col = RandT<T>::randexp(&rs) / seff[cell];
+            T dist_col = kF32 ? RandT<T>::randexp(&rs) * rseff[cell] : RandT<T>::randexp(&rs) / seff[cell];
             T dist_cen = c * (dtT - t) * ds;
             T dist = jmin(jmin(dist_b, dist_col), dist_cen);
             if (dist != dist) { s.flags |= IMC_FLAG_NAN; p.alive = false; break; }
-            T newenergy = energy * std::exp(-saf[cell] * dist);
+            const T edens = kF32 ? energy * rarea[cell] : (energy / dxT[xi]) / dyT[yi];
+            T newenergy, dep;
+            if (kF32) {
+                const T em1 = std::expm1(-saf[cell] * dist);
+                newenergy = energy + energy * em1;
+                dep = -edens * em1;
+            } else {
+                newenergy = energy * std::exp(-saf[cell] * dist);
+                dep = -edens * std::expm1(-saf[cell] * dist);
+            }
             if (newenergy <= minenergy) {
-                dep_add(s, k, cell, (double)((energy / dxT[xi]) / dyT[yi]));
+                dep_add(s, k, cell, (double)edens);
                 p.alive = false;
                 break;
             }
-            dep_add(s, k, cell, (double)(-((energy / dxT[xi]) / dyT[yi]) * std::expm1(-saf[cell] * dist)));
+            dep_add(s, k, cell, (double)dep);
             xp += dist * vx;
             yp += dist * vy;
-            t += (dist / ds) / c;
+            if (kF32) t += dist * rdsc;
+            else t += (dist / ds) / c;
             energy = newenergy;
             if (dist == dist_bx || dist == dist_by) {
                 bool killed = false;
