@@ -237,16 +237,39 @@ IMC_HD bool fix_place(uint64_t man, int sh, bool neg, Limbs &o) {
     return true;
 }
 
+IMC_HD int bitlen32(uint32_t m) {
+#ifdef __CUDA_ARCH__
+    return 32 - __clz((int)m);
+#else
+    return m ? 32 - __builtin_clz(m) : 0;
+#endif
+}
+
+// FP32 values: the 24-bit mantissa lands in at most two of the three 32-bit
+// words, placed with 32-bit shifts (the same result as fix_place).
 IMC_HD bool fix_split(float v, int b, Limbs &o) {
     uint32_t bits = f2u(v);
     bool neg = (bits >> 31) != 0;
     int ex = (int)((bits >> 23) & 0xFFu);
     if (ex == 0xFF) return false;
-    uint64_t man = bits & 0x7FFFFFu;
+    uint32_t man = bits & 0x7FFFFFu;
     int e2;
     if (ex == 0) e2 = 1 - 127 - 23;
     else { man |= 0x800000u; e2 = ex - 127 - 23; }
-    return fix_place(man, e2 - b, neg, o);
+    const int sh = e2 - b;
+    if (sh < 0 || man == 0) return fix_place(man, sh, neg, o);
+    if (bitlen32(man) + sh > 94) return false;
+    const int w = sh >> 5, off = sh & 31;
+    const uint32_t lo = man << off;
+    const uint32_t hi = off ? man >> (32 - off) : 0u;
+    uint32_t w0 = 0u, w1 = 0u, w2 = 0u;  // bits 0-31, 32-63, 64-95
+    if (w == 0) { w0 = lo; w1 = hi; }
+    else if (w == 1) { w1 = lo; w2 = hi; }
+    else { w2 = lo; }
+    long long l2 = (long long)w0, l1 = (long long)w1, l0 = (long long)w2;
+    if (neg) { l0 = -l0; l1 = -l1; l2 = -l2; }
+    o.l0 = l0; o.l1 = l1; o.l2 = l2;
+    return true;
 }
 IMC_HD bool fix_split(double v, int b, Limbs &o) {
     uint64_t bits = d2u(v);

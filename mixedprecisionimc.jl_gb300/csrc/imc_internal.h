@@ -40,6 +40,7 @@ struct Scalars {
     double n_source;                   // particle budget of this step
     unsigned long long segments;
     unsigned long long surrogate_calls;
+    float seg_per_hist;                // segments per history of the last transport
     unsigned long long qcount[2 * kSurrRounds + 1];  // surrogate transport: ask queue of round r at 2r, resume queue at 2r + 1
     unsigned int flags;
     int b_dep, b_rad, b_lost;          // fixed-point exponents of this transport

@@ -709,6 +709,10 @@ __global__ void __launch_bounds__(kCellThreads) k_finalize(CellArgs ca, Scalars 
             d[0] = d[1] = d[2] = 0;
         }
         sc->lost_step = lost;
+        // mean transport segments per history of this step: the next
+        // transport picks its lane schedule from it
+        const double hist = (double)(sc->n_census_in + sc->n_sourced);
+        sc->seg_per_hist = hist > 0.0 ? (float)((double)sc->segments / hist) : 0.0f;
         sc->lostenergy += lost;
     }
 }

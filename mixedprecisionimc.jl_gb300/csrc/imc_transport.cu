@@ -24,6 +24,9 @@
 
 namespace imc {
 
+// segments per history at and above which the 1D kernel refills lanes
+constexpr float kRefillSegments = 3.0f;
+
 template <class St, int BLOCK, bool SMT>
 __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc, PBufPair bufs) {
     typedef typename St::T T;
@@ -55,128 +58,218 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     unsigned flags = 0;
     T emax = (T)0;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        if (!pb.alive[i]) continue;
-        const int cs = pb.cs[i];
-        int cell = cs & 0xFFFFFF;
-        const int k = cs >> 24;
-        T t, x, mu, E;
-        const T E0 = (T)pb.E0[i];
-        if (St::half) {
-            t = ld_f(pb.t + i) * (float)endsteptime;
-            x = ld_f(pb.x + i) * (float)tab[cell].dxs;
-            mu = ld_f(pb.ux + i);
-            E = ld_f(pb.E + i) * (float)E0;
-        } else {
-            t = (T)pb.t[i]; x = (T)pb.x[i]; mu = (T)pb.ux[i]; E = (T)pb.E[i];
-        }
-        Stream rs;
+    // Lane state of the history in flight.
+    long long i = 0;
+    int cs = 0, cell = 0, k = 0, acc_cell = 0;
+    T t = (T)0, x = (T)0, mu = (T)0, E = (T)0, E0 = (T)0, minenergy = (T)0, acc_s = (T)0, acc_c = (T)0, rmu = (T)0;
+    long long seg = 0;
+    Stream rs;
+    auto start = [&]() {
+        cell = cs & 0xFFFFFF;
+        k = cs >> 24;
         rs.init(seed, step, (uint32_t)i, kStageTransport);
-        const T minenergy = (T)(0.01 * (double)E0);
-        T acc_s = (T)0, acc_c = (T)0;
-        int acc_cell = cell;
-        long long seg = 0;
-        int end = 0;  // 1 killed / escaped, 2 census
-        T rmu = (T)1 / mu;  // FP32: the face distance as a product (reset at each new direction)
-        while (!end) {
-            // one pass of the reference's while loop (src/imc_transport.jl:73-195)
-            if (++seg > cap) {
-                flags |= (1u << 2);
+        minenergy = (T)(0.01 * (double)E0);
+        acc_s = (T)0;
+        acc_c = (T)0;
+        acc_cell = cell;
+        seg = 0;
+        rmu = (T)1 / mu;  // FP32: the face distance as a product (reset at each new direction)
+    };
+    // one pass of the reference's while loop; 0 = go on, 1 = killed or
+    // escaped, 2 = census
+    auto segment = [&]() -> int {
+        int end = 0;
+        // one pass of the reference's while loop (src/imc_transport.jl:73-195)
+        if (++seg > cap) {
+            flags |= (1u << 2);
+            end = 1;
+        } else {
+            const Tab1<T> ce = tab[cell];
+            T dist_b;
+            if constexpr (sizeof(T) == 4) dist_b = mu > (T)0 ? (ce.dxs - x) * rmu : m_abs(x * rmu);
+            else dist_b = mu > (T)0 ? (ce.dxs - x) / mu : m_abs(x / mu);
+            const T dist_col = M::flight(rs, ce);
+            const T dist_cen = c * (endsteptime - t) * ds;
+            const T dist = jmin(jmin(dist_b, dist_col), dist_cen);
+            if (dist != dist) {
+                flags |= 1u;
                 end = 1;
             } else {
-                const Tab1<T> ce = tab[cell];
-                T dist_b;
-                if constexpr (sizeof(T) == 4) dist_b = mu > (T)0 ? (ce.dxs - x) * rmu : m_abs(x * rmu);
-                else dist_b = mu > (T)0 ? (ce.dxs - x) / mu : m_abs(x / mu);
-                const T dist_col = M::flight(rs, ce);
-                const T dist_cen = c * (endsteptime - t) * ds;
-                const T dist = jmin(jmin(dist_b, dist_col), dist_cen);
-                if (dist != dist) {
-                    flags |= 1u;
+                T dep;
+                const T newenergy = M::attenuate(E, ce, dist, &dep);
+                if (cell != acc_cell) {
+                    flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+                    acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
+                }
+                if (newenergy <= minenergy) {
+                    nadd(acc_s, acc_c, M::all_in(E, ce));
                     end = 1;
                 } else {
-                    T dep;
-                    const T newenergy = M::attenuate(E, ce, dist, &dep);
-                    if (cell != acc_cell) {
-                        flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
-                        acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
-                    }
-                    if (newenergy <= minenergy) {
-                        nadd(acc_s, acc_c, M::all_in(E, ce));
-                        end = 1;
-                    } else {
-                        nadd(acc_s, acc_c, dep);
-                        x += mu * dist;
-                        if constexpr (sizeof(T) == 4) t += dist * rdsc;
-                        else t += (ds_one ? dist : dist / ds) / c;
-                        E = newenergy;
-                        if (dist == dist_b) {
-                            if (mu > (T)0) {
-                                if (cell == N - 1) {
-                                    if (reflect_r) {
-                                        mu = -mu;
-                                        rmu = -rmu;
-                                    } else {
-                                        flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
-                                        end = 1;
-                                    }
-                                }
-                                if (!end) {
-                                    cell += 1;
-                                    x = (T)0;
-                                }
-                            }
-                            if (!end && mu < (T)0) {
-                                if (cell == 0) {
-                                    if (reflect_l) {
-                                        mu = -mu;
-                                        rmu = -rmu;
-                                    } else {
-                                        flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
-                                        end = 1;
-                                    }
+                    nadd(acc_s, acc_c, dep);
+                    x += mu * dist;
+                    if constexpr (sizeof(T) == 4) t += dist * rdsc;
+                    else t += (ds_one ? dist : dist / ds) / c;
+                    E = newenergy;
+                    if (dist == dist_b) {
+                        if (mu > (T)0) {
+                            if (cell == N - 1) {
+                                if (reflect_r) {
+                                    mu = -mu;
+                                    rmu = -rmu;
                                 } else {
-                                    cell -= 1;
-                                    x = tab[cell].dxs;
+                                    flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
+                                    end = 1;
                                 }
                             }
-                        }
-                        if (!end && dist == dist_col) {
-                            // mu = 1 - 2*rand, redrawn while zero (src/imc_transport.jl:178-181);
-                            // a zero needs rand == 0.5 exactly, so 64 redraws never run out
-                            mu = (T)0;
-                            for (int r = 0; r < 64 && mu == (T)0; ++r) mu = (T)1 - (T)2 * Rand<T>::u(rs);
-                            if (mu == (T)0) mu = (T)1;
-                            rmu = (T)1 / mu;
-                        }
-                        if (!end && dist == dist_cen) {
-                            // census: t = 0, write the state back (src/imc_transport.jl:185-193)
-                            T Est = E;
-                            if (St::half) {
-                                st_v(pb.t + i, 0.0f);
-                                st_v(pb.x + i, (float)x / (float)tab[cell].dxs);
-                                st_v(pb.ux + i, (float)mu);
-                                __half ef = __float2half_rn((float)E / (float)E0);
-                                pb.E[i] = ef;
-                                Est = __half2float(ef) * (float)E0;
-                            } else {
-                                pb.t[i] = (typename St::S)0;
-                                pb.x[i] = (typename St::S)x;
-                                pb.ux[i] = (typename St::S)mu;
-                                pb.E[i] = (typename St::S)E;
+                            if (!end) {
+                                cell += 1;
+                                x = (T)0;
                             }
-                            if (cell != (cs & 0xFFFFFF)) pb.cs[i] = cell | (k << 24);
-                            flush_one<T, SMT>(rad_acc, k * nc + cell, Est, b_rad, flags);
-                            emax = Est > emax ? Est : emax;
-                            end = 2;
                         }
+                        if (!end && mu < (T)0) {
+                            if (cell == 0) {
+                                if (reflect_l) {
+                                    mu = -mu;
+                                    rmu = -rmu;
+                                } else {
+                                    flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
+                                    end = 1;
+                                }
+                            } else {
+                                cell -= 1;
+                                x = tab[cell].dxs;
+                            }
+                        }
+                    }
+                    if (!end && dist == dist_col) {
+                        // mu = 1 - 2*rand, redrawn while zero (src/imc_transport.jl:178-181);
+                        // a zero needs rand == 0.5 exactly, so 64 redraws never run out
+                        mu = (T)0;
+                        for (int r = 0; r < 64 && mu == (T)0; ++r) mu = (T)1 - (T)2 * Rand<T>::u(rs);
+                        if (mu == (T)0) mu = (T)1;
+                        rmu = (T)1 / mu;
+                    }
+                    if (!end && dist == dist_cen) {
+                        // census: t = 0, write the state back (src/imc_transport.jl:185-193)
+                        T Est = E;
+                        if (St::half) {
+                            st_v(pb.t + i, 0.0f);
+                            st_v(pb.x + i, (float)x / (float)tab[cell].dxs);
+                            st_v(pb.ux + i, (float)mu);
+                            __half ef = __float2half_rn((float)E / (float)E0);
+                            pb.E[i] = ef;
+                            Est = __half2float(ef) * (float)E0;
+                        } else {
+                            pb.t[i] = (typename St::S)0;
+                            pb.x[i] = (typename St::S)x;
+                            pb.ux[i] = (typename St::S)mu;
+                            pb.E[i] = (typename St::S)E;
+                        }
+                        if (cell != (cs & 0xFFFFFF)) pb.cs[i] = cell | (k << 24);
+                        flush_one<T, SMT>(rad_acc, k * nc + cell, Est, b_rad, flags);
+                        emax = Est > emax ? Est : emax;
+                        end = 2;
                     }
                 }
             }
         }
+        return end;
+    };
+    auto finish = [&](int end) {
         flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
         if (end == 1) pb.alive[i] = 0;
         segs += (unsigned long long)seg;
+    };
+    const int lane = threadIdx.x & 31;
+    if (sc->seg_per_hist < kRefillSegments) {
+        // Short histories (the last transport averaged fewer than
+        // kRefillSegments segments each): each lane walks one history to its
+        // end, and the warp moves on together to 32 consecutive entries, so
+        // every load and store of the list is coalesced.
+        for (i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            if (!pb.alive[i]) continue;
+            cs = pb.cs[i];
+            E0 = (T)pb.E0[i];
+            if (St::half) {
+                t = ld_f(pb.t + i) * (float)endsteptime;
+                x = ld_f(pb.x + i) * (float)tab[cs & 0xFFFFFF].dxs;
+                mu = ld_f(pb.ux + i);
+                E = ld_f(pb.E + i) * (float)E0;
+            } else {
+                t = (T)pb.t[i]; x = (T)pb.x[i]; mu = (T)pb.ux[i]; E = (T)pb.E[i];
+            }
+            start();
+            int end;
+            do end = segment(); while (!end);
+            finish(end);
+        }
+    } else {
+        // Long histories of unequal length: each lane starts the next history
+        // as soon as its current one ends.  The warp reads the list in chunks
+        // of 32 consecutive entries (coalesced: lane l prefetches entry
+        // 32 c + l into registers); idle lanes take the chunk's entries in
+        // order through register shuffles.
+        const unsigned lt = (1u << lane) - 1u;
+        const long long nchunks = (n + 31) / 32;
+        const long long cstride = (long long)gridDim.x * (BLOCK / 32);
+        long long chunk = (long long)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
+        int p_cs = -1;  // prefetched entry (-1: none / dead)
+        T p_t = (T)0, p_x = (T)0, p_mu = (T)0, p_E = (T)0, p_E0 = (T)0;
+        auto prefetch = [&]() {
+            const long long j = chunk * 32 + lane;
+            p_cs = -1;
+            if (j < n && pb.alive[j]) {
+                p_cs = pb.cs[j];
+                p_E0 = (T)pb.E0[j];
+                if (St::half) {
+                    p_t = ld_f(pb.t + j) * (float)endsteptime;
+                    p_x = ld_f(pb.x + j) * (float)tab[p_cs & 0xFFFFFF].dxs;
+                    p_mu = ld_f(pb.ux + j);
+                    p_E = ld_f(pb.E + j) * (float)p_E0;
+                } else {
+                    p_t = (T)pb.t[j]; p_x = (T)pb.x[j]; p_mu = (T)pb.ux[j]; p_E = (T)pb.E[j];
+                }
+            }
+        };
+        bool more = chunk < nchunks;  // warp-uniform: the current chunk has entries left
+        int pos = 0;                  // warp-uniform: next entry of the chunk to hand out
+        if (more) prefetch();
+        bool has = false;
+        while (true) {
+            unsigned idle = __ballot_sync(0xFFFFFFFFu, !has);
+            while (idle && more) {
+                const int r = __popc(idle & lt);
+                const int avail = 32 - pos;
+                const int sl = (pos + r) & 31;
+                const int q_cs = __shfl_sync(0xFFFFFFFFu, p_cs, sl);
+                const T q_t = __shfl_sync(0xFFFFFFFFu, p_t, sl), q_x = __shfl_sync(0xFFFFFFFFu, p_x, sl);
+                const T q_mu = __shfl_sync(0xFFFFFFFFu, p_mu, sl), q_E = __shfl_sync(0xFFFFFFFFu, p_E, sl);
+                const T q_E0 = __shfl_sync(0xFFFFFFFFu, p_E0, sl);
+                if (!has && r < avail && q_cs >= 0) {
+                    i = chunk * 32 + pos + r;
+                    cs = q_cs;
+                    t = q_t; x = q_x; mu = q_mu; E = q_E; E0 = q_E0;
+                    start();
+                    has = true;
+                }
+                const int nidle = __popc(idle);
+                pos += nidle < avail ? nidle : avail;
+                if (pos >= 32) {
+                    chunk += cstride;
+                    more = chunk < nchunks;
+                    pos = 0;
+                    if (more) prefetch();
+                }
+                idle = __ballot_sync(0xFFFFFFFFu, !has);
+            }
+            if (idle == 0xFFFFFFFFu) break;  // no history left for this warp
+            if (!has) continue;
+            const int end = segment();
+            if (end) {
+                finish(end);
+                has = false;
+            }
+        }
     }
     if (SMT) flush_block_tallies(ca, dep_acc);
     finish_counters<T>(sc, segs, flags, emax);
