@@ -62,6 +62,10 @@ DECKS = {
            "left segment y in [0,0.5] at T=0.5, dt=1e-3 to t=1, NINPUT=1e7, NMAX=5e7, FP32 state",
            None),
 }
+# DRAM traffic of the transport kernel per algorithmic byte, from one ncu
+# capture of the half-size slab launch (bench.py --profile): 393.9 MB read +
+# written for ~410 MB of algorithmic bytes
+TRAFFIC_PER_ALGO_BYTE = 393.9 / 410.0
 DECK_KEY = "c2"
 DECK = os.path.join(GOLDEN, "decks", DECKS[DECK_KEY][0])
 REF_MEAN = os.path.join(GOLDEN, DECKS[DECK_KEY][2])
@@ -410,7 +414,11 @@ def main():
     avg_ms = tr_ms / max(tr_n, 1)
     achieved = bytes_per_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": (achieved / hbm) if (achieved and hbm) else None, "traffic": None,
+                "frac": (achieved / hbm) if (achieved and hbm) else None,
+                "traffic": TRAFFIC_PER_ALGO_BYTE * bytes_per_launch if DECK_KEY == "c2" else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the half-size slab "
+                                  "launch (393.9 MB for ~410 MB algorithmic), scaled to this launch's "
+                                  "algorithmic bytes",
                 "kernel": "k_transport2d<StF32>" if DECK_KEY == "c4" else "k_transport1d<StF32>", "avg_launch_ms": avg_ms, "launches": tr_n,
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "transport_share_of_step": tr_ms / dev_ms if dev_ms else None,
