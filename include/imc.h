@@ -219,7 +219,23 @@ int imc_step(ImcHandle *h, ImcStepStats *stats, int *done);
 int imc_run(ImcHandle *h, int64_t max_steps, ImcStepStats *stats,
             int64_t *n_steps, double *device_ms);
 
+/* Batched ensemble: runs every handle to the end of its clock (at most
+ * max_steps steps each), `n_threads` host threads driving the handles' own
+ * CUDA streams, so the decks' kernels run side by side on the GPU (each
+ * handle's transport grid is sized to its particle buffer).  Handles must be
+ * distinct.  steps[i] (optional) = steps run by handle i; *wall_ms (optional)
+ * = host wall time of the whole batch.  Returns IMC_OK or the status of the
+ * first handle that failed, whose index goes to *failed (-1 if none). */
+int imc_run_batch(ImcHandle *const *hs, int32_t n, int64_t max_steps, int32_t n_threads, int64_t *steps,
+                  double *wall_ms, int32_t *failed);
+
+/* Totals over every step run by imc_step / imc_run since imc_create:
+ * segments, histories (census carried in + births, per step) and surrogate
+ * queries; any pointer may be NULL. */
+int imc_get_totals(const ImcHandle *h, int64_t *segments, int64_t *histories, int64_t *surrogate_calls);
+
 /* ---- state access ------------------------------------------------------- */
+
 
 /* simulation clock (simvars.t, simvars.dt) and step counter */
 int imc_get_time(const ImcHandle *h, double *t, double *dt, int64_t *step_index);

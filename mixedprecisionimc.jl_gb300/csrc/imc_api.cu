@@ -12,6 +12,10 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <mutex>
+#include <thread>
+#include <chrono>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -49,6 +53,7 @@ struct ImcHandle {
     DevStats *d_stats = nullptr;
     long long stats_cap = 0;
     int grid_transport = 0, block_transport = 256, grid_emit = 0;
+    int grid_full = 0;  // resident transport blocks on the whole GPU
     // learned surrogate: device image of the network (ca.surr_image points
     // into it while the surrogate is on) and its kernel's persistent grid
     void *d_surr_image = nullptr;
@@ -66,6 +71,8 @@ struct ImcHandle {
     double t = 0.0, dt = 0.0;
     int64_t step = 0;
     bool finished = false;
+    // totals over every step run since imc_create
+    int64_t tot_segments = 0, tot_histories = 0, tot_calls = 0;
     int stage = Stage::Fresh;
     long long n_census_host = 0;
     ImcStepStats last{};
@@ -104,11 +111,25 @@ template <class T> int dalloc(ImcHandle *h, T **p, size_t n, std::vector<void *>
     return IMC_OK;
 }
 
+// Synchronous copy on the handle's own stream (never the legacy default
+// stream), so handles driven from different host threads -- one of them
+// possibly capturing its step graph -- do not interact.
+cudaError_t hcopy(const ImcHandle *h, void *dst, const void *src, size_t bytes, cudaMemcpyKind kind) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, h->stream);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(h->stream);
+}
+cudaError_t hset(const ImcHandle *h, void *dst, int v, size_t bytes) {
+    cudaError_t e = cudaMemsetAsync(dst, v, bytes, h->stream);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(h->stream);
+}
+
 template <class T> int upload(ImcHandle *h, T **p, const T *src, size_t n) {
     int rc = dalloc(h, p, n, h->allocs);
     if (rc) return rc;
-    if (src && n) CK(h, cudaMemcpy(*p, src, n * sizeof(T), cudaMemcpyHostToDevice));
-    else CK(h, cudaMemset(*p, 0, std::max<size_t>(n, 1) * sizeof(T)));
+    if (src && n) CK(h, hcopy(h, *p, src, n * sizeof(T), cudaMemcpyHostToDevice));
+    else CK(h, hset(h, *p, 0, std::max<size_t>(n, 1) * sizeof(T)));
     return IMC_OK;
 }
 
@@ -143,6 +164,14 @@ void free_list(std::vector<void *> &list) {
 
 void drop_graphs(ImcHandle *h) {
     if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+}
+
+// Transport blocks for this handle: the resident grid of the whole GPU, or
+// fewer for a small particle buffer (16 entries per thread at capacity), so
+// that the kernels of small decks run side by side in a batch.
+int sized_grid(const ImcHandle *h, int full, int block) {
+    const long long want = (h->capacity + 16ll * block - 1) / (16ll * block);
+    return (int)std::max<long long>(1, std::min<long long>(full, want));
 }
 
 PBufPair pair(const ImcHandle *h) {
@@ -204,7 +233,7 @@ int grow(ImcHandle *h, long long need) {
     long long ncap = std::max<long long>(need + need / 2, h->capacity + h->capacity / 2);
     CK(h, cudaStreamSynchronize(h->stream));
     Scalars sc;
-    CK(h, cudaMemcpy(&sc, h->d_sc, sizeof(Scalars), cudaMemcpyDeviceToHost));
+    CK(h, hcopy(h, &sc, h->d_sc, sizeof(Scalars), cudaMemcpyDeviceToHost));
     const long long n = sc.n_particles;
     PBufRaw nb[2];
     std::vector<void *> nlist;
@@ -216,25 +245,26 @@ int grow(ImcHandle *h, long long need) {
     const PBufRaw &o = h->buf[sc.cur];
     PBufRaw &w = nb[0];
     if (n > 0) {
-        CK(h, cudaMemcpy(w.t, o.t, se * n, cudaMemcpyDeviceToDevice));
-        CK(h, cudaMemcpy(w.x, o.x, se * n, cudaMemcpyDeviceToDevice));
-        CK(h, cudaMemcpy(w.ux, o.ux, se * n, cudaMemcpyDeviceToDevice));
+        CK(h, hcopy(h, w.t, o.t, se * n, cudaMemcpyDeviceToDevice));
+        CK(h, hcopy(h, w.x, o.x, se * n, cudaMemcpyDeviceToDevice));
+        CK(h, hcopy(h, w.ux, o.ux, se * n, cudaMemcpyDeviceToDevice));
         if (h->geometry == 2) {
-            CK(h, cudaMemcpy(w.y, o.y, se * n, cudaMemcpyDeviceToDevice));
-            CK(h, cudaMemcpy(w.uy, o.uy, se * n, cudaMemcpyDeviceToDevice));
+            CK(h, hcopy(h, w.y, o.y, se * n, cudaMemcpyDeviceToDevice));
+            CK(h, hcopy(h, w.uy, o.uy, se * n, cudaMemcpyDeviceToDevice));
         }
-        CK(h, cudaMemcpy(w.E, o.E, se * n, cudaMemcpyDeviceToDevice));
-        CK(h, cudaMemcpy(w.E0, o.E0, e0 * n, cudaMemcpyDeviceToDevice));
-        CK(h, cudaMemcpy(w.cs, o.cs, 4 * n, cudaMemcpyDeviceToDevice));
-        CK(h, cudaMemcpy(w.alive, o.alive, n, cudaMemcpyDeviceToDevice));
+        CK(h, hcopy(h, w.E, o.E, se * n, cudaMemcpyDeviceToDevice));
+        CK(h, hcopy(h, w.E0, o.E0, e0 * n, cudaMemcpyDeviceToDevice));
+        CK(h, hcopy(h, w.cs, o.cs, 4 * n, cudaMemcpyDeviceToDevice));
+        CK(h, hcopy(h, w.alive, o.alive, n, cudaMemcpyDeviceToDevice));
     }
     free_list(h->pallocs);
     h->pallocs = nlist;
     h->buf[0] = nb[0];
     h->buf[1] = nb[1];
     sc.cur = 0;
-    CK(h, cudaMemcpy(h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice));
+    CK(h, hcopy(h, h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice));
     h->ca.capacity = ncap;
+    h->grid_transport = sized_grid(h, h->grid_full, h->block_transport);
     if ((rc = tile_alloc(h))) return rc;
     if (h->ca.surr_image && (rc = surr_queue_alloc(h))) return rc;
     drop_graphs(h);
@@ -293,7 +323,12 @@ void host_timestep(const ImcDeck &d, double &t, double &dt, bool &finished) {
 
 // the transport kernel of this handle: analog, or with the learned surrogate
 void run_transport(ImcHandle *h, PBufPair bufs, cudaStream_t st) {
-    if (h->ca.surr_image) launch_transport_surr(h->ca, h->d_sc, h->prec, bufs, h->wave, h->sshape, st);
+    if (h->ca.surr_image) {
+        SurrShapes sh = h->sshape;
+        sh.analog_grid = sized_grid(h, sh.analog_grid, sh.analog_block);
+        sh.query_grid = sized_grid(h, sh.query_grid, sh.query_block);
+        launch_transport_surr(h->ca, h->d_sc, h->prec, bufs, h->wave, sh, st);
+    }
     else launch_transport(h->ca, h->d_sc, h->prec, bufs, h->grid_transport, st);
 }
 
@@ -347,8 +382,24 @@ int ensure_stats(ImcHandle *h, long long n) {
     return IMC_OK;
 }
 
+std::mutex g_capture_mutex;  // one step-graph capture at a time in the process
+std::mutex g_attr_mutex;     // kernel attributes are per process, shared by every handle
+
+// Raises a kernel's dynamic shared-memory limit to at least `smem`, never
+// lowering it: handles of different meshes share the kernel, and a handle
+// created later must not shrink the limit under one that runs now.
+cudaError_t raise_smem_limit(const void *kp, int smem) {
+    std::lock_guard<std::mutex> lock(g_attr_mutex);
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, kp);
+    if (e != cudaSuccess) return e;
+    if (smem <= a.maxDynamicSharedSizeBytes) return cudaSuccess;
+    return cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
 int capture(ImcHandle *h) {
     if (h->graph) return IMC_OK;
+    std::lock_guard<std::mutex> lock(g_capture_mutex);
     cudaGraph_t g;
     CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     int rc = enqueue_step(h, false, 0);
@@ -521,7 +572,7 @@ int imc_create(const ImcDeck *d, ImcHandle **out) {
     if (cudaMalloc(&q, sizeof(Scalars)) != cudaSuccess) return bail(fail(h, IMC_ERR_OOM, "cudaMalloc scalars"));
     h->allocs.push_back(q);
     h->d_sc = (Scalars *)q;
-    if (cudaMemcpy(h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice) != cudaSuccess)
+    if (hcopy(h, h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(fail(h, IMC_ERR_CUDA, "upload scalars"));
     if ((rc = ensure_stats(h, 64))) return bail(rc);
     // launch shapes: persistent grids sized by occupancy on this GPU
@@ -531,12 +582,13 @@ int imc_create(const ImcDeck *d, ImcHandle **out) {
     const void *kp = transport_kernel_ptr(ca, h->prec);
     if (smem > 227 * 1024) return bail(fail(h, IMC_ERR_INVALID_ARG, "mesh too large for the shared-memory transport table"));
     if (smem > 48 * 1024)
-        if (cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        if (raise_smem_limit(kp, smem) != cudaSuccess)
             return bail(fail(h, IMC_ERR_CUDA, "cudaFuncSetAttribute(smem)"));
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp, h->block_transport, smem) != cudaSuccess || per_sm < 1)
         return bail(fail(h, IMC_ERR_CUDA, "transport kernel cannot be resident"));
-    h->grid_transport = h->sm_count * per_sm;
+    h->grid_full = h->sm_count * per_sm;
+    h->grid_transport = sized_grid(h, h->grid_full, h->block_transport);
     h->grid_emit = h->sm_count * 4;
     if (cudaEventCreate(&h->ev[0]) != cudaSuccess || cudaEventCreate(&h->ev[1]) != cudaSuccess)
         return bail(fail(h, IMC_ERR_CUDA, "cudaEventCreate"));
@@ -633,7 +685,7 @@ int imc_energycheck(ImcHandle *h, double *energy_error) {
     int rc = read_scalars(h, &sc);
     if (rc) return rc;
     DevStats ds;
-    CK(h, cudaMemcpy(&ds, h->d_stats + (sc.step % (unsigned long long)h->stats_cap), sizeof(DevStats),
+    CK(h, hcopy(h, &ds, h->d_stats + (sc.step % (unsigned long long)h->stats_cap), sizeof(DevStats),
                      cudaMemcpyDeviceToHost));
     to_stats(ds, &h->last);
     if (energy_error) *energy_error = sc.energy_err;
@@ -672,9 +724,12 @@ int imc_step(ImcHandle *h, ImcStepStats *stats, int *done) {
     if ((rc = read_scalars(h, &sc))) return rc;
     if (h->timing && (rc = collect_events(h, 1))) return rc;
     DevStats ds;
-    CK(h, cudaMemcpy(&ds, h->d_stats + ((sc.step - 1u) % (unsigned long long)h->stats_cap), sizeof(DevStats),
+    CK(h, hcopy(h, &ds, h->d_stats + ((sc.step - 1u) % (unsigned long long)h->stats_cap), sizeof(DevStats),
                      cudaMemcpyDeviceToHost));
     to_stats(ds, &h->last);
+    h->tot_segments += ds.segments;
+    h->tot_histories += ds.n_census_in + ds.n_sourced;
+    h->tot_calls += ds.surrogate_calls;
     if (stats) *stats = h->last;
     bool fin;
     host_timestep(h->deck, h->t, h->dt, fin);
@@ -749,12 +804,15 @@ int imc_run(ImcHandle *h, int64_t max_steps, ImcStepStats *stats, int64_t *n_ste
     std::vector<DevStats> ds((size_t)done_steps);
     for (int64_t s = 0; s < done_steps; ++s) {
         unsigned long long slot = (slot0 + (unsigned long long)s) % (unsigned long long)h->stats_cap;
-        CK(h, cudaMemcpy(&ds[s], h->d_stats + slot, sizeof(DevStats), cudaMemcpyDeviceToHost));
+        CK(h, hcopy(h, &ds[s], h->d_stats + slot, sizeof(DevStats), cudaMemcpyDeviceToHost));
     }
     unsigned allflags = 0;
     for (int64_t s = 0; s < done_steps; ++s) {
         if (stats) to_stats(ds[s], &stats[s]);
         allflags |= ds[s].error_flags;
+        h->tot_segments += ds[s].segments;
+        h->tot_histories += ds[s].n_census_in + ds[s].n_sourced;
+        h->tot_calls += ds[s].surrogate_calls;
         bool fin;
         host_timestep(h->deck, h->t, h->dt, fin);
         h->finished = fin;
@@ -764,6 +822,53 @@ int imc_run(ImcHandle *h, int64_t max_steps, ImcStepStats *stats, int64_t *n_ste
     h->stage = Stage::Fresh;
     if (n_steps) *n_steps = done_steps;
     return flags_status(h, allflags);
+}
+
+int imc_run_batch(ImcHandle *const *hs, int32_t n, int64_t max_steps, int32_t n_threads, int64_t *steps,
+                  double *wall_ms, int32_t *failed) {
+    if (!hs || n < 0 || n_threads < 1) return IMC_ERR_INVALID_ARG;
+    for (int32_t i = 0; i < n; ++i)
+        if (!hs[i]) return IMC_ERR_INVALID_ARG;
+    for (int32_t i = 0; i < n; ++i)
+        for (int32_t j = 0; j < i; ++j)
+            if (hs[i] == hs[j]) return IMC_ERR_INVALID_ARG;  // a handle is not thread-safe
+    if (failed) *failed = -1;
+    std::atomic<int32_t> next(0);
+    std::atomic<int> first_rc(IMC_OK);
+    std::atomic<int32_t> first_bad(-1);
+    auto worker = [&]() {
+        while (true) {
+            const int32_t i = next.fetch_add(1);
+            if (i >= n) return;
+            ImcHandle *h = hs[i];
+            int64_t st = 0;
+            int rc = cudaSetDevice(h->device) == cudaSuccess ? imc_run(h, max_steps, nullptr, &st, nullptr)
+                                                             : fail(h, IMC_ERR_CUDA, "cudaSetDevice");
+            if (steps) steps[i] = st;
+            if (rc != IMC_OK) {
+                int expect = IMC_OK;
+                if (first_rc.compare_exchange_strong(expect, rc)) first_bad.store(i);
+            }
+        }
+    };
+    const auto t0 = std::chrono::steady_clock::now();
+    const int nt = (int)std::min<int32_t>(n_threads, std::max<int32_t>(n, 1));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto &th : pool) th.join();
+    const auto t1 = std::chrono::steady_clock::now();
+    if (wall_ms) *wall_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    if (failed) *failed = first_bad.load();
+    return first_rc.load();
+}
+
+int imc_get_totals(const ImcHandle *h, int64_t *segments, int64_t *histories, int64_t *surrogate_calls) {
+    if (!h) return IMC_ERR_INVALID_ARG;
+    if (segments) *segments = h->tot_segments;
+    if (histories) *histories = h->tot_histories;
+    if (surrogate_calls) *surrogate_calls = h->tot_calls;
+    return IMC_OK;
 }
 
 int imc_get_time(const ImcHandle *h, double *t, double *dt, int64_t *step_index) {
@@ -781,7 +886,7 @@ int imc_set_time(ImcHandle *h, double t, double dt) {
     if (rc) return rc;
     sc.t = t; sc.dt = dt;
     sc.finished = t > h->deck.t_end ? 1 : 0;
-    CK(h, cudaMemcpy(h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice));
+    CK(h, hcopy(h, h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice));
     h->t = t; h->dt = dt; h->finished = t > h->deck.t_end;
     return IMC_OK;
 }
@@ -821,7 +926,7 @@ int imc_get_field(const ImcHandle *h, int field, double *out, int64_t count) {
     if (!p) return fail(hh, IMC_ERR_INVALID_ARG, "unknown field");
     if (n != count) return fail(hh, IMC_ERR_INVALID_ARG, "field size mismatch");
     CK(hh, cudaStreamSynchronize(h->stream));
-    CK(hh, cudaMemcpy(out, p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    CK(hh, hcopy(hh, out, p, sizeof(double) * n, cudaMemcpyDeviceToHost));
     return IMC_OK;
 }
 
@@ -832,7 +937,7 @@ int imc_set_field(ImcHandle *h, int field, const double *in, int64_t count) {
     if (!p) return fail(h, IMC_ERR_INVALID_ARG, "unknown field");
     if (n != count) return fail(h, IMC_ERR_INVALID_ARG, "field size mismatch");
     CK(h, cudaStreamSynchronize(h->stream));
-    CK(h, cudaMemcpy(p, in, sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(h, hcopy(h, p, in, sizeof(double) * n, cudaMemcpyHostToDevice));
     return IMC_OK;
 }
 
@@ -850,17 +955,17 @@ int imc_get_particles(const ImcHandle *hc, ImcParticles *p) {
     std::vector<int32_t> cs(n);
     std::vector<uint8_t> alive(n);
     if (n > 0) {
-        CK(h, cudaMemcpy(t.data(), b.t, se * n, cudaMemcpyDeviceToHost));
-        CK(h, cudaMemcpy(x.data(), b.x, se * n, cudaMemcpyDeviceToHost));
-        CK(h, cudaMemcpy(ux.data(), b.ux, se * n, cudaMemcpyDeviceToHost));
+        CK(h, hcopy(h, t.data(), b.t, se * n, cudaMemcpyDeviceToHost));
+        CK(h, hcopy(h, x.data(), b.x, se * n, cudaMemcpyDeviceToHost));
+        CK(h, hcopy(h, ux.data(), b.ux, se * n, cudaMemcpyDeviceToHost));
         if (h->geometry == 2) {
-            CK(h, cudaMemcpy(y.data(), b.y, se * n, cudaMemcpyDeviceToHost));
-            CK(h, cudaMemcpy(uy.data(), b.uy, se * n, cudaMemcpyDeviceToHost));
+            CK(h, hcopy(h, y.data(), b.y, se * n, cudaMemcpyDeviceToHost));
+            CK(h, hcopy(h, uy.data(), b.uy, se * n, cudaMemcpyDeviceToHost));
         }
-        CK(h, cudaMemcpy(E.data(), b.E, se * n, cudaMemcpyDeviceToHost));
-        CK(h, cudaMemcpy(E0.data(), b.E0, e0 * n, cudaMemcpyDeviceToHost));
-        CK(h, cudaMemcpy(cs.data(), b.cs, 4 * n, cudaMemcpyDeviceToHost));
-        CK(h, cudaMemcpy(alive.data(), b.alive, n, cudaMemcpyDeviceToHost));
+        CK(h, hcopy(h, E.data(), b.E, se * n, cudaMemcpyDeviceToHost));
+        CK(h, hcopy(h, E0.data(), b.E0, e0 * n, cudaMemcpyDeviceToHost));
+        CK(h, hcopy(h, cs.data(), b.cs, 4 * n, cudaMemcpyDeviceToHost));
+        CK(h, hcopy(h, alive.data(), b.alive, n, cudaMemcpyDeviceToHost));
     }
     auto rd = [&](const std::vector<unsigned char> &v, long long i) -> double {
         if (h->prec == 0) return ((const double *)v.data())[i];
@@ -950,17 +1055,17 @@ int imc_set_particles(ImcHandle *h, const ImcParticles *p) {
     if ((rc = read_scalars(h, &sc))) return rc;
     const PBufRaw &b = h->buf[sc.cur];
     if (n > 0) {
-        CK(h, cudaMemcpy(b.t, t.data(), se * n, cudaMemcpyHostToDevice));
-        CK(h, cudaMemcpy(b.x, x.data(), se * n, cudaMemcpyHostToDevice));
-        CK(h, cudaMemcpy(b.ux, ux.data(), se * n, cudaMemcpyHostToDevice));
+        CK(h, hcopy(h, b.t, t.data(), se * n, cudaMemcpyHostToDevice));
+        CK(h, hcopy(h, b.x, x.data(), se * n, cudaMemcpyHostToDevice));
+        CK(h, hcopy(h, b.ux, ux.data(), se * n, cudaMemcpyHostToDevice));
         if (h->geometry == 2) {
-            CK(h, cudaMemcpy(b.y, y.data(), se * n, cudaMemcpyHostToDevice));
-            CK(h, cudaMemcpy(b.uy, uy.data(), se * n, cudaMemcpyHostToDevice));
+            CK(h, hcopy(h, b.y, y.data(), se * n, cudaMemcpyHostToDevice));
+            CK(h, hcopy(h, b.uy, uy.data(), se * n, cudaMemcpyHostToDevice));
         }
-        CK(h, cudaMemcpy(b.E, E.data(), se * n, cudaMemcpyHostToDevice));
-        CK(h, cudaMemcpy(b.E0, E0.data(), e0s * n, cudaMemcpyHostToDevice));
-        CK(h, cudaMemcpy(b.cs, cs.data(), 4 * n, cudaMemcpyHostToDevice));
-        CK(h, cudaMemcpy(b.alive, alive.data(), n, cudaMemcpyHostToDevice));
+        CK(h, hcopy(h, b.E, E.data(), se * n, cudaMemcpyHostToDevice));
+        CK(h, hcopy(h, b.E0, E0.data(), e0s * n, cudaMemcpyHostToDevice));
+        CK(h, hcopy(h, b.cs, cs.data(), 4 * n, cudaMemcpyHostToDevice));
+        CK(h, hcopy(h, b.alive, alive.data(), n, cudaMemcpyHostToDevice));
     }
     long long live = 0;
     for (long long i = 0; i < n; ++i) live += alive[i];
@@ -969,7 +1074,7 @@ int imc_set_particles(ImcHandle *h, const ImcParticles *p) {
     union { double d; unsigned long long u; } cv;
     cv.d = emax;
     sc.emax_census_bits = cv.u;
-    CK(h, cudaMemcpy(h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice));
+    CK(h, hcopy(h, h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice));
     h->stage = Stage::Fresh;
     return IMC_OK;
 }
@@ -1029,7 +1134,7 @@ int imc_set_surrogate(ImcHandle *h, const float *params, int64_t n_params) {
         const void *kp = surr_kernel_ptr(ca, h->prec, which);
         const int block = which == 3 ? sh.query_block : sh.analog_block;
         const int smem = which == 3 ? sh.query_smem : sh.analog_smem;
-        CK(h, cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        CK(h, raise_smem_limit(kp, smem));
         int per_sm = 0;
         CK(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp, block, smem));
         if (per_sm < 1) return fail(h, IMC_ERR_CUDA, "surrogate transport kernel cannot be resident");

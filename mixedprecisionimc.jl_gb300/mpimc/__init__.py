@@ -9,5 +9,5 @@ sm_103a kernels.
 from . import Constants, Input, Mesh, Utilities  # noqa: F401
 from . import Clean, EnergyCheck, Sourcing, Tally, Transport, Update  # noqa: F401
 from .driver import ParticleList, RunResult, SimVars, main, make_simvars, timestep  # noqa: F401
-from .engine import Engine, build_deck, device_info  # noqa: F401
+from .engine import Engine, build_deck, device_info, run_batch  # noqa: F401
 from ._lib import ImcError  # noqa: F401

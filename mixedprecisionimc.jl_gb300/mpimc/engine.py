@@ -273,6 +273,12 @@ class Engine:
         self._c(self.lib.imc_get_stats(self.h, C.byref(st)))
         return st.as_dict()
 
+    def totals(self):
+        """(segments, histories, surrogate calls) over every step run so far."""
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        self._c(self.lib.imc_get_totals(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
     def set_surrogate(self, params):
         """Turn the learned thick-cell surrogate on (FP32 parameters from
         mpimc.surrogate.train) or off (None); 1D, FP32 / FP16 state."""
@@ -309,3 +315,20 @@ def device_info():
     rc = lib.imc_device_info(name, 256, C.byref(sm), C.byref(ma), C.byref(mi))
     check(rc, None, lib)
     return {"name": name.value.decode(), "sm_count": sm.value, "cc": (ma.value, mi.value)}
+
+
+def run_batch(engines, max_steps=1 << 40, threads=16):
+    """Batched ensemble (imc_run_batch): runs every Engine to the end of its
+    clock, the decks' kernels side by side on the GPU.  Returns (steps per
+    engine, host wall seconds).  Raises ImcError naming the first failure."""
+    lib = _lib.load()
+    n = len(engines)
+    hs = (C.c_void_p * max(n, 1))(*[e.h for e in engines])
+    steps = (C.c_int64 * max(n, 1))()
+    wall = C.c_double()
+    bad = C.c_int32(-1)
+    rc = lib.imc_run_batch(hs, n, max_steps, threads, steps, C.byref(wall), C.byref(bad))
+    if rc != _lib.IMC_OK:
+        e = engines[bad.value] if bad.value >= 0 else None
+        check(rc, e.h if e else None, lib)
+    return [steps[i] for i in range(n)], wall.value / 1000.0
