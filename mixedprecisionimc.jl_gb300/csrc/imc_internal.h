@@ -132,6 +132,12 @@ struct SurrShapes {
     int query_block, query_smem, query_grid;     // query passes
 };
 SurrShapes surr_shapes(const CellArgs &ca, int prec);
+// the analog passes are the 1D transport kernel in its pass modes
+// (imc_transport.cu); which: 0 list pass, 1 resume pass, 2 last resume pass
+const void *surr_analog_ptr(const CellArgs &ca, int prec, int which);
+int surr_analog_smem(const CellArgs &ca, int prec);
+void launch_surr_analog(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, const SurrWave &w, int which,
+                        int round, int grid, int smem, cudaStream_t st);
 // kernel pointers for attribute / occupancy set-up: which = 0 list pass,
 // 1 resume pass that sets aside, 2 last resume pass, 3 query pass
 const void *surr_kernel_ptr(const CellArgs &ca, int prec, int which);

@@ -27,10 +27,21 @@ namespace imc {
 // segments per history at and above which the 1D kernel refills lanes
 constexpr float kRefillSegments = 3.0f;
 
-template <class St, int BLOCK, bool SMT>
-__global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc, PBufPair bufs) {
+// 1D analog kernel modes: the plain transport, and the passes of the
+// surrogate transport (imc_transport_surr.cu) -- the list pass and the resume
+// passes set aside histories that want a network query; the last resume
+// pass walks everything to its end.
+enum { kModePlain = 0, kModeList = 1, kModeResume = 2, kModeResumeLast = 3 };
+
+template <class St, int BLOCK, bool SMT, int MODE>
+__global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc, PBufPair bufs, SurrWave w,
+                                                       int round) {
     typedef typename St::T T;
     typedef SegMath<T> M;
+    constexpr bool kFromQueue = MODE == kModeResume || MODE == kModeResumeLast;
+    constexpr bool kPause = MODE == kModeList || MODE == kModeResume;
+    const long long n = kFromQueue ? (long long)sc->qcount[2 * round + 1] : sc->n_particles;
+    if (kFromQueue && n == 0) return;
     PBuf<St> pb(bufs.b[sc->cur]);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Tab1<T> *tab = reinterpret_cast<Tab1<T> *>(smem_raw);
@@ -44,30 +55,34 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         rad_acc = dep_acc + 3 * (size_t)ca.K * ca.nc;
         for (int i = threadIdx.x; i < 6 * ca.K * ca.nc; i += blockDim.x) dep_acc[i] = 0;
     }
-    for (int i = threadIdx.x; i < N; i += blockDim.x) tab[i] = make_tab1<T>(ca.sa[i], ca.fleck[i], ca.ss[i], ca.dx[i], ds);
-    __syncthreads();
     const T endsteptime = (T)sc->dt;
-    const long long n = sc->n_particles;
+    float *gate = reinterpret_cast<float *>(smem_raw + analog1d_smem(ca, sizeof(T), SMT, false));
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tab[i] = make_tab1<T>(ca.sa[i], ca.fleck[i], ca.ss[i], ca.dx[i], ds);
+    if (kPause) fill_gate<T>(ca, gate, ds, c, endsteptime);
+    __syncthreads();
     const int b_dep = sc->b_dep, b_rad = sc->b_rad, b_lost = sc->b_lost;
     const unsigned step = sc->step;
     const unsigned long long seed = ca.seed;
     const long long cap = ca.seg_cap;
     const int nc = ca.nc;
     const bool reflect_r = ca.bc[1] == 1, reflect_l = ca.bc[0] == 1;
-    unsigned long long segs = 0;
+    unsigned long long *ask_count = &sc->qcount[kFromQueue ? 2 * round + 2 : 0];
+    const uint32_t stage = kFromQueue ? kStageResume + (uint32_t)round : kStageTransport;
+    unsigned long long segs = 0, calls = 0;
     unsigned flags = 0;
     T emax = (T)0;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    // Lane state of the history in flight.
+    // Lane state of the history in flight (cs: as stored in the list; the
+    // current cell and scale are cell, k).
     long long i = 0;
     int cs = 0, cell = 0, k = 0, acc_cell = 0;
     T t = (T)0, x = (T)0, mu = (T)0, E = (T)0, E0 = (T)0, minenergy = (T)0, acc_s = (T)0, acc_c = (T)0, rmu = (T)0;
     long long seg = 0;
     Stream rs;
-    auto start = [&]() {
-        cell = cs & 0xFFFFFF;
-        k = cs >> 24;
-        rs.init(seed, step, (uint32_t)i, kStageTransport);
+    auto start = [&](int cs_now) {
+        cell = cs_now & 0xFFFFFF;
+        k = cs_now >> 24;
+        rs.init(seed, step, (uint32_t)i, stage);
         minenergy = (T)(0.01 * (double)E0);
         acc_s = (T)0;
         acc_c = (T)0;
@@ -75,9 +90,48 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         seg = 0;
         rmu = (T)1 / mu;  // FP32: the face distance as a product (reset at each new direction)
     };
+    // one entry of the list (or of the resume queue): false if it holds no history
+    auto load = [&](long long e, int &cs_now, T &lt, T &lx, T &lmu, T &lE, T &lE0, long long &li, int &lcs) -> bool {
+        if (kFromQueue) {
+            li = w.resume.idx[e];
+            lcs = w.resume.cs_list[e];
+            cs_now = w.resume.cs[e];
+            lt = (T)w.resume.t[e]; lx = (T)w.resume.x[e]; lmu = (T)w.resume.mu[e];
+            lE = (T)w.resume.E[e]; lE0 = (T)w.resume.E0[e];
+            return true;
+        }
+        if (!pb.alive[e]) return false;
+        li = e;
+        lcs = cs_now = pb.cs[e];
+        lE0 = (T)pb.E0[e];
+        if (St::half) {
+            lt = ld_f(pb.t + e) * (float)endsteptime;
+            lx = ld_f(pb.x + e) * (float)tab[cs_now & 0xFFFFFF].dxs;
+            lmu = ld_f(pb.ux + e);
+            lE = ld_f(pb.E + e) * (float)lE0;
+        } else {
+            lt = (T)pb.t[e]; lx = (T)pb.x[e]; lmu = (T)pb.ux[e]; lE = (T)pb.E[e];
+        }
+        return true;
+    };
     // one pass of the reference's while loop; 0 = go on, 1 = killed or
-    // escaped, 2 = census
+    // escaped, 2 = census, 3 = set aside for a query (kPause)
     auto segment = [&]() -> int {
+        if (kPause && (float)(x < tab[cell].dxs - x ? x : tab[cell].dxs - x) * (float)tab[cell].seff >= gate[cell]) {
+            Query q;
+            const int kind = surr_decide<T>(tab[cell], x, mu, t, E, minenergy, c, ds, endsteptime, q);
+            if (kind == kCertainKill) {
+                if (cell != acc_cell) {
+                    flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+                    acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
+                }
+                nadd(acc_s, acc_c, M::all_in(E, tab[cell]));
+                ++seg;
+                ++calls;
+                return 1;
+            }
+            if (kind == kAsk) return 3;
+        }
         int end = 0;
         // one pass of the reference's while loop (src/imc_transport.jl:73-195)
         if (++seg > cap) {
@@ -177,7 +231,14 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     };
     auto finish = [&](int end) {
         flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
-        if (end == 1) pb.alive[i] = 0;
+        if (end == 3) {
+            // set aside with its state for the query pass (its deposits flushed)
+            const unsigned long long j = atomicAdd(ask_count, 1ull);
+            w.ask.x[j] = (float)x; w.ask.mu[j] = (float)mu; w.ask.t[j] = (float)t; w.ask.E[j] = (float)E;
+            w.ask.E0[j] = (float)E0; w.ask.cs[j] = cell | (k << 24); w.ask.cs_list[j] = cs; w.ask.idx[j] = i;
+        } else if (end == 1) {
+            pb.alive[i] = 0;
+        }
         segs += (unsigned long long)seg;
     };
     const int lane = threadIdx.x & 31;
@@ -186,49 +247,33 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         // kRefillSegments segments each): each lane walks one history to its
         // end, and the warp moves on together to 32 consecutive entries, so
         // every load and store of the list is coalesced.
-        for (i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-            if (!pb.alive[i]) continue;
-            cs = pb.cs[i];
-            E0 = (T)pb.E0[i];
-            if (St::half) {
-                t = ld_f(pb.t + i) * (float)endsteptime;
-                x = ld_f(pb.x + i) * (float)tab[cs & 0xFFFFFF].dxs;
-                mu = ld_f(pb.ux + i);
-                E = ld_f(pb.E + i) * (float)E0;
-            } else {
-                t = (T)pb.t[i]; x = (T)pb.x[i]; mu = (T)pb.ux[i]; E = (T)pb.E[i];
-            }
-            start();
+        for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+            int cs_now;
+            if (!load(e, cs_now, t, x, mu, E, E0, i, cs)) continue;
+            start(cs_now);
             int end;
             do end = segment(); while (!end);
             finish(end);
         }
     } else {
         // Long histories of unequal length: each lane starts the next history
-        // as soon as its current one ends.  The warp reads the list in chunks
-        // of 32 consecutive entries (coalesced: lane l prefetches entry
-        // 32 c + l into registers); idle lanes take the chunk's entries in
-        // order through register shuffles.
+        // as soon as its current one ends.  The warp reads the entries in
+        // chunks of 32 (coalesced: lane l prefetches entry 32 c + l into
+        // registers); idle lanes take the chunk's entries in order through
+        // register shuffles.
         const unsigned lt = (1u << lane) - 1u;
         const long long nchunks = (n + 31) / 32;
         const long long cstride = (long long)gridDim.x * (BLOCK / 32);
         long long chunk = (long long)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
-        int p_cs = -1;  // prefetched entry (-1: none / dead)
+        int p_now = -1, p_cs = 0;  // prefetched entry (p_now -1: none / dead)
+        long long p_i = 0;
         T p_t = (T)0, p_x = (T)0, p_mu = (T)0, p_E = (T)0, p_E0 = (T)0;
         auto prefetch = [&]() {
-            const long long j = chunk * 32 + lane;
-            p_cs = -1;
-            if (j < n && pb.alive[j]) {
-                p_cs = pb.cs[j];
-                p_E0 = (T)pb.E0[j];
-                if (St::half) {
-                    p_t = ld_f(pb.t + j) * (float)endsteptime;
-                    p_x = ld_f(pb.x + j) * (float)tab[p_cs & 0xFFFFFF].dxs;
-                    p_mu = ld_f(pb.ux + j);
-                    p_E = ld_f(pb.E + j) * (float)p_E0;
-                } else {
-                    p_t = (T)pb.t[j]; p_x = (T)pb.x[j]; p_mu = (T)pb.ux[j]; p_E = (T)pb.E[j];
-                }
+            const long long e = chunk * 32 + lane;
+            p_now = -1;
+            if (e < n) {
+                int cn;
+                if (load(e, cn, p_t, p_x, p_mu, p_E, p_E0, p_i, p_cs)) p_now = cn;
             }
         };
         bool more = chunk < nchunks;  // warp-uniform: the current chunk has entries left
@@ -241,15 +286,17 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
                 const int r = __popc(idle & lt);
                 const int avail = 32 - pos;
                 const int sl = (pos + r) & 31;
+                const int q_now = __shfl_sync(0xFFFFFFFFu, p_now, sl);
                 const int q_cs = __shfl_sync(0xFFFFFFFFu, p_cs, sl);
+                const long long q_i = __shfl_sync(0xFFFFFFFFu, p_i, sl);
                 const T q_t = __shfl_sync(0xFFFFFFFFu, p_t, sl), q_x = __shfl_sync(0xFFFFFFFFu, p_x, sl);
                 const T q_mu = __shfl_sync(0xFFFFFFFFu, p_mu, sl), q_E = __shfl_sync(0xFFFFFFFFu, p_E, sl);
                 const T q_E0 = __shfl_sync(0xFFFFFFFFu, p_E0, sl);
-                if (!has && r < avail && q_cs >= 0) {
-                    i = chunk * 32 + pos + r;
+                if (!has && r < avail && q_now >= 0) {
+                    i = q_i;
                     cs = q_cs;
                     t = q_t; x = q_x; mu = q_mu; E = q_E; E0 = q_E0;
-                    start();
+                    start(q_now);
                     has = true;
                 }
                 const int nidle = __popc(idle);
@@ -272,6 +319,10 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         }
     }
     if (SMT) flush_block_tallies(ca, dep_acc);
+    if (kPause) {
+        for (int off = 16; off > 0; off >>= 1) calls += __shfl_down_sync(0xFFFFFFFFu, calls, off);
+        if (lane == 0 && calls) atomicAdd(&sc->surrogate_calls, calls);
+    }
     finish_counters<T>(sc, segs, flags, emax);
 }
 
@@ -490,7 +541,8 @@ TransportShape transport_shape(const CellArgs &ca, int prec) {
 }
 
 template <class St, int B, bool SMT> static const void *kptr(int geometry) {
-    return geometry == 1 ? (const void *)k_transport1d<St, B, SMT> : (const void *)k_transport2d<St, B, SMT>;
+    return geometry == 1 ? (const void *)k_transport1d<St, B, SMT, kModePlain>
+                         : (const void *)k_transport2d<St, B, SMT>;
 }
 
 const void *transport_kernel_ptr(const CellArgs &ca, int prec) {
@@ -507,7 +559,7 @@ const void *transport_kernel_ptr(const CellArgs &ca, int prec) {
 
 template <class St, int B, bool SMT>
 static void launch_one(const CellArgs &ca, Scalars *sc, PBufPair buf, int grid, int smem, cudaStream_t st) {
-    if (ca.geometry == 1) k_transport1d<St, B, SMT><<<grid, B, smem, st>>>(ca, sc, buf);
+    if (ca.geometry == 1) k_transport1d<St, B, SMT, kModePlain><<<grid, B, smem, st>>>(ca, sc, buf, SurrWave{}, 0);
     else k_transport2d<St, B, SMT><<<grid, B, smem, st>>>(ca, sc, buf);
 }
 
@@ -521,6 +573,44 @@ void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufPair buf, i
         if (prec == 0) launch_one<StF64, 256, false>(ca, sc, buf, grid, sh.smem, st);
         else if (prec == 1) launch_one<StF32, 256, false>(ca, sc, buf, grid, sh.smem, st);
         else launch_one<StF16, 256, false>(ca, sc, buf, grid, sh.smem, st);
+    }
+}
+
+// ------------------------------------------- analog passes of the surrogate transport
+// which: 0 the list pass, 1 a resume pass that sets aside, 2 the last resume pass
+template <class St, int B, bool SMT> static const void *wave_ptr(int which) {
+    if (which == 0) return (const void *)k_transport1d<St, B, SMT, kModeList>;
+    if (which == 1) return (const void *)k_transport1d<St, B, SMT, kModeResume>;
+    return (const void *)k_transport1d<St, B, SMT, kModeResumeLast>;
+}
+
+const void *surr_analog_ptr(const CellArgs &ca, int prec, int which) {
+    const bool smt = transport_shape(ca, prec).smem_tally;
+    if (prec == 2) return smt ? wave_ptr<StF16, kSmtBlock32, true>(which) : wave_ptr<StF16, 256, false>(which);
+    return smt ? wave_ptr<StF32, kSmtBlock32, true>(which) : wave_ptr<StF32, 256, false>(which);
+}
+
+int surr_analog_smem(const CellArgs &ca, int prec) {
+    return analog1d_smem(ca, 4, transport_shape(ca, prec).smem_tally, true);
+}
+
+template <class St, int B, bool SMT>
+static void wave_one(const CellArgs &ca, Scalars *sc, PBufPair bufs, const SurrWave &w, int which, int round,
+                     int grid, int smem, cudaStream_t st) {
+    if (which == 0) k_transport1d<St, B, SMT, kModeList><<<grid, B, smem, st>>>(ca, sc, bufs, w, round);
+    else if (which == 1) k_transport1d<St, B, SMT, kModeResume><<<grid, B, smem, st>>>(ca, sc, bufs, w, round);
+    else k_transport1d<St, B, SMT, kModeResumeLast><<<grid, B, smem, st>>>(ca, sc, bufs, w, round);
+}
+
+void launch_surr_analog(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, const SurrWave &w, int which,
+                        int round, int grid, int smem, cudaStream_t st) {
+    const bool smt = transport_shape(ca, prec).smem_tally;
+    if (prec == 2) {
+        if (smt) wave_one<StF16, kSmtBlock32, true>(ca, sc, bufs, w, which, round, grid, smem, st);
+        else wave_one<StF16, 256, false>(ca, sc, bufs, w, which, round, grid, smem, st);
+    } else {
+        if (smt) wave_one<StF32, kSmtBlock32, true>(ca, sc, bufs, w, which, round, grid, smem, st);
+        else wave_one<StF32, 256, false>(ca, sc, bufs, w, which, round, grid, smem, st);
     }
 }
 

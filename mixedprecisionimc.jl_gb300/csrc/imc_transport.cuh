@@ -8,6 +8,7 @@
 #include "imc_device.cuh"
 #include "imc_internal.h"
 #include "imc_state.cuh"
+#include "imc_surrogate.cuh"
 
 namespace imc {
 
@@ -176,6 +177,70 @@ __device__ __forceinline__ void finish_counters(Scalars *sc, unsigned long long 
         if (flags) atomicOr(&sc->flags, flags);
         if (em > 0.0) atomicMax(&sc->emax_census_bits, (unsigned long long)d2u(em));
     }
+}
+
+// ------------------------------------------------ learned surrogate: when to ask
+// The walk's state in mean free paths, for the network (imc_surrogate.cuh).
+struct Query {
+    float W, dn, df, mup, L;
+    bool near_left;  // the nearer face is the left one
+    bool cut;        // the 1 % energy cut-off ends the walk at L (truncation = kill)
+    bool census;     // census ends the walk at L
+};
+
+enum { kAnalog = 0, kAsk = 1, kCertainKill = 2 };
+
+// Whether a history at (x, mu, t, E) in a cell should walk analog, ask the
+// network, or die here for certain (no face within reach before the cut-off).
+template <class T>
+__device__ __forceinline__ int surr_decide(const Tab1<T> &ce, T x, T mu, T t, T E, T minenergy, T c, T ds, T dt,
+                                           Query &q) {
+    using namespace surr;
+    const float seff = (float)ce.seff;
+    const float W = (float)ce.dxs * seff;
+    if (!(W >= kCellMin)) return kAnalog;
+    const float lcen = seff * (float)(c * (dt - t) * ds);
+    const float lcut = ce.saf > (T)0 ? logf((float)E / (float)minenergy) * seff / (float)ce.saf : INFINITY;
+    const float L = fminf(lcen, lcut);
+    if (!(L >= kLmaxMin)) return kAnalog;
+    const float xm = (float)x * seff;
+    q.W = W;
+    q.near_left = xm <= 0.5f * W;
+    q.dn = fmaxf(q.near_left ? xm : W - xm, 0.0f);
+    q.df = W - q.dn;
+    q.mup = q.near_left ? (float)mu : -(float)mu;
+    q.cut = lcut <= lcen && lcut <= kLmaxMax;
+    q.census = !q.cut && lcen <= kLmaxMax;
+    q.L = fminf(L, kLmaxMax);
+    if (q.cut && q.dn >= q.L) return kCertainKill;
+    return expected_collisions(q.dn, q.df, q.L) >= kMinGain ? kAsk : kAnalog;
+}
+
+// Per-cell gate of the analog passes: the least distance from the nearer
+// face, in mean free paths, at which a history of this cell can want a query
+// this step (infinity where none can: cell narrower than kCellMin mean free
+// paths, or lmax below kMinGain even at the step's start with full energy).
+// With lmax at most Lc = min(census path seff c dt ds, cut-off path
+// ln(100) seff / (sigma_a f)), asking needs 1.95 d_n sqrt(Lc) >= kMinGain,
+// so histories nearer the face than kMinGain / (1.95 sqrt(Lc)) skip the test.
+template <class T>
+__device__ __forceinline__ void fill_gate(const CellArgs &ca, float *gate, T ds, T c, T dt) {
+    using namespace surr;
+    for (int i = threadIdx.x; i < ca.nx; i += blockDim.x) {
+        const float sa = (float)ca.sa[i], f = (float)ca.fleck[i], ss = (float)ca.ss[i];
+        const float saf = sa * f, seff = sa * (1.0f - f) + ss;
+        const float W = (float)ca.dx[i] * (float)ds * seff;
+        const float lcen = seff * (float)(c * dt * ds);
+        const float lcut = saf > 0.0f ? 4.6051702f * seff / saf : INFINITY;
+        const float Lc = fminf(lcen, lcut);
+        gate[i] = (W >= kCellMin && Lc >= kMinGain) ? kMinGain / (1.95f * sqrtf(Lc)) : INFINITY;
+    }
+}
+
+// shared-memory bytes of the 1D analog kernel: table, private tallies (SMT),
+// and the per-cell gate when histories may be set aside for queries
+__host__ __device__ __forceinline__ int analog1d_smem(const CellArgs &ca, int tsz, bool smt, bool gate) {
+    return table_bytes(ca, tsz) + (smt ? 48 * ca.K * ca.nc : 0) + (gate ? ((4 * ca.nx + 15) & ~15) : 0);
 }
 
 }  // namespace imc

@@ -18,17 +18,17 @@
 // analog segments want every lane walking its own history.  So a step runs
 // as separate passes (all launched on the stream, replayed in the step's
 // CUDA graph):
-//   k_wave_analog (list)   the analog kernel over the particle list; a
-//                          history that wants a query flushes its deposits
-//                          and is set aside in the `ask` queue
+//   list pass              the 1D transport kernel (imc_transport.cu) in its
+//                          list mode: a history that wants a query flushes
+//                          its deposits and is set aside in the `ask` queue
 //   k_wave_query (round r) every queued history gets one query, 32 per warp
 //                          (two MMA passes of 16 rows, all lanes sampling);
 //                          census, kill and escape finish the history,
 //                          face exits and 1e4-path pieces continue in the
 //                          `resume` queue
-//   k_wave_analog (resume) the analog kernel over the resume queue, which
-//                          may set histories aside again, except in the
-//                          last of kSurrRounds rounds
+//   resume pass            the 1D transport kernel over the resume queue,
+//                          which may set histories aside again, except in
+//                          the last of kSurrRounds rounds
 // A resumed history draws from its own Philox stream per round (stage tags
 // kStageResume + r, kStageQuery + r), so results do not depend on the order
 // of the queues, which atomics fill; tallies are exact fixed-point sums.
@@ -58,30 +58,6 @@ template <class T> struct Hist {
     long long seg;
     Stream rs;
 };
-
-template <class St, class T>
-__device__ __forceinline__ void load_hist(const PBuf<St> &pb, const Tab1<T> *tab, long long i, T dt,
-                                          unsigned long long seed, unsigned step, Hist<T> &h) {
-    h.i = i;
-    h.cs = pb.cs[i];
-    h.cell = h.cs & 0xFFFFFF;
-    h.k = h.cs >> 24;
-    h.E0 = (T)pb.E0[i];
-    if (St::half) {
-        h.t = ld_f(pb.t + i) * (float)dt;
-        h.x = ld_f(pb.x + i) * (float)tab[h.cell].dxs;
-        h.mu = ld_f(pb.ux + i);
-        h.E = ld_f(pb.E + i) * (float)h.E0;
-    } else {
-        h.t = (T)pb.t[i]; h.x = (T)pb.x[i]; h.mu = (T)pb.ux[i]; h.E = (T)pb.E[i];
-    }
-    h.rs.init(seed, step, (uint32_t)i, kStageTransport);
-    h.minenergy = (T)(0.01 * (double)h.E0);
-    h.acc_s = (T)0;
-    h.acc_c = (T)0;
-    h.acc_cell = h.cell;
-    h.seg = 0;
-}
 
 // census: write the state back (src/imc_transport.jl:185-193) and tally it
 template <class St, class T, bool SMT>
@@ -155,71 +131,9 @@ __device__ __forceinline__ void follow_cell(Hist<T> &h, long long *dep_acc, int 
 
 enum { kGo = 0, kKilled = 1, kCensus = 2, kPaused = 3 };
 
-// one analog segment of k_transport1d (src/imc_transport.jl:72-193)
-template <class T, bool SMT>
-__device__ __forceinline__ int analog_segment(const CellArgs &ca, const Tab1<T> *tab, Hist<T> &h, T c, T ds,
-                                              bool ds_one, T dt, long long cap, int N, bool reflect_l, bool reflect_r,
-                                              long long *dep_acc, int nc, int b_dep, int b_lost, unsigned &flags) {
-    if (++h.seg > cap) { flags |= (1u << 2); return kKilled; }
-    const Tab1<T> ce = tab[h.cell];
-    const T dist_b = h.mu > (T)0 ? (ce.dxs - h.x) / h.mu : m_abs(h.x / h.mu);
-    const T dist_col = SegMath<T>::flight(h.rs, ce);
-    const T dist_cen = c * (dt - h.t) * ds;
-    const T dist = jmin(jmin(dist_b, dist_col), dist_cen);
-    if (dist != dist) { flags |= 1u; return kKilled; }
-    T dep;
-    const T newenergy = SegMath<T>::attenuate(h.E, ce, dist, &dep);
-    follow_cell<T, SMT>(h, dep_acc, nc, b_dep, flags);
-    if (newenergy <= h.minenergy) {
-        nadd(h.acc_s, h.acc_c, SegMath<T>::all_in(h.E, ce));
-        return kKilled;
-    }
-    nadd(h.acc_s, h.acc_c, dep);
-    h.x += h.mu * dist;
-    h.t += (ds_one ? dist : dist / ds) / c;
-    h.E = newenergy;
-    if (dist == dist_b)
-        if (!cross_face<T>(ca, tab, h, N, reflect_l, reflect_r, b_lost, flags)) return kKilled;
-    if (dist == dist_col) {
-        h.mu = (T)0;
-        for (int r = 0; r < 64 && h.mu == (T)0; ++r) h.mu = (T)1 - (T)2 * Rand<T>::u(h.rs);
-        if (h.mu == (T)0) h.mu = (T)1;
-    }
-    if (dist == dist_cen) return kCensus;
-    return kGo;
-}
-
-// the walk's state in mean free paths, for the network
-struct Query {
-    float W, dn, df, mup, L;
-    bool near_left;  // the nearer face is the left one
-    bool cut;        // the 1 % energy cut-off ends the walk at L (truncation = kill)
-    bool census;     // census ends the walk at L
-};
-
-enum { kAnalog = 0, kAsk = 1, kCertainKill = 2 };
-
 template <class T>
 __device__ __forceinline__ int decide(const Tab1<T> &ce, const Hist<T> &h, T c, T ds, T dt, Query &q) {
-    const float seff = (float)ce.seff;
-    const float W = (float)ce.dxs * seff;
-    if (!(W >= kCellMin)) return kAnalog;
-    const float lcen = seff * (float)(c * (dt - h.t) * ds);
-    const float lcut = ce.saf > (T)0 ? logf((float)h.E / (float)h.minenergy) * seff / (float)ce.saf : INFINITY;
-    const float L = fminf(lcen, lcut);
-    if (!(L >= kLmaxMin)) return kAnalog;
-    const float xm = (float)h.x * seff;
-    q.W = W;
-    q.near_left = xm <= 0.5f * W;
-    q.dn = fmaxf(q.near_left ? xm : W - xm, 0.0f);
-    q.df = W - q.dn;
-    q.mup = q.near_left ? (float)h.mu : -(float)h.mu;
-    q.cut = lcut <= lcen && lcut <= kLmaxMax;
-    q.census = !q.cut && lcen <= kLmaxMax;
-    q.L = fminf(L, kLmaxMax);
-    // no face within reach before the cut-off: the history dies in this cell
-    if (q.cut && q.dn >= q.L) return kCertainKill;
-    return expected_collisions(q.dn, q.df, q.L) >= kMinGain ? kAsk : kAnalog;
+    return surr_decide<T>(ce, h.x, h.mu, h.t, h.E, h.minenergy, c, ds, dt, q);
 }
 
 // applies a sampled outcome (cls, y0, y1) of the walk described by q
@@ -309,121 +223,6 @@ __device__ __forceinline__ void load_queued(const SurrQueue &qq, long long e, un
 template <class T>
 __device__ __forceinline__ void fill_table(const CellArgs &ca, Tab1<T> *tab, T ds) {
     for (int i = threadIdx.x; i < ca.nx; i += blockDim.x) tab[i] = make_tab1<T>(ca.sa[i], ca.fleck[i], ca.ss[i], ca.dx[i], ds);
-}
-
-// Per-cell gate of the analog passes: 0 where no history can want a query
-// this step -- cell narrower than kCellMin mean free paths, or lmax below
-// kMinGain even at the step's start with full energy (census path
-// seff c dt ds, cut-off path ln(100) seff / (sigma_a f)).
-template <class T>
-__device__ __forceinline__ void fill_gate(const CellArgs &ca, uint8_t *gate, T ds, T c, T dt) {
-    for (int i = threadIdx.x; i < ca.nx; i += blockDim.x) {
-        const float sa = (float)ca.sa[i], f = (float)ca.fleck[i], ss = (float)ca.ss[i];
-        const float saf = sa * f, seff = sa * (1.0f - f) + ss;
-        const float W = (float)ca.dx[i] * (float)ds * seff;
-        const float lcen = seff * (float)(c * dt * ds);
-        const float lcut = saf > 0.0f ? 4.6051702f * seff / saf : INFINITY;
-        gate[i] = (W >= kCellMin && fminf(lcen, lcut) >= kMinGain) ? 1 : 0;
-    }
-}
-
-// Walks a history analog until it ends (kCensus / kKilled) or, with pause,
-// until it wants a query (kPaused, its deposits flushed).  A certain kill ends
-// it at once.
-template <class T, bool SMT>
-__device__ __forceinline__ int walk_analog(const CellArgs &ca, const Tab1<T> *tab, const uint8_t *gate, Hist<T> &h,
-                                           bool pause, T c, T ds,
-                                           bool ds_one, T dt, long long cap, int N, bool reflect_l, bool reflect_r,
-                                           long long *dep_acc, int nc, int b_dep, int b_lost, unsigned &flags,
-                                           unsigned long long &calls) {
-    int res = kGo;
-    while (true) {
-        if (pause && gate[h.cell]) {
-            const Tab1<T> ce = tab[h.cell];
-            {
-                Query q;
-                const int kind = decide<T>(ce, h, c, ds, dt, q);
-                if (kind == kCertainKill) {
-                    follow_cell<T, SMT>(h, dep_acc, nc, b_dep, flags);
-                    nadd(h.acc_s, h.acc_c, SegMath<T>::all_in(h.E, ce));
-                    h.seg += 1;
-                    calls += 1;
-                    res = kKilled;
-                    break;
-                }
-                if (kind == kAsk) {
-                    res = kPaused;
-                    break;
-                }
-            }
-        }
-        res = analog_segment<T, SMT>(ca, tab, h, c, ds, ds_one, dt, cap, N, reflect_l, reflect_r, dep_acc, nc, b_dep,
-                                     b_lost, flags);
-        if (res != kGo) break;
-    }
-    flush_pair<T, SMT>(dep_acc, h.k * nc + h.acc_cell, h.acc_s, h.acc_c, b_dep, flags);
-    h.acc_s = (T)0;
-    h.acc_c = (T)0;
-    return res;
-}
-
-// ------------------------------------------------------------ analog pass
-// The analog kernel over the list (IN_Q = false; its pauses fill the ask
-// queue of round 0) or over the resume queue of round `round` (IN_Q = true;
-// with PAUSE its pauses fill the ask queue of round + 1).
-template <class St, int BLOCK, bool SMT, bool IN_Q, bool PAUSE>
-__global__ void __launch_bounds__(BLOCK) k_wave_analog(CellArgs ca, Scalars *sc, PBufPair bufs, SurrWave w,
-                                                       int round) {
-    typedef typename St::T T;
-    const long long n = IN_Q ? (long long)sc->qcount[2 * round + 1] : sc->n_particles;
-    if (n == 0) return;
-    PBuf<St> pb(bufs.b[sc->cur]);
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    Tab1<T> *tab = reinterpret_cast<Tab1<T> *>(smem_raw);
-    const int N = ca.nx, nc = ca.nc;
-    const T ds = (T)ca.ds, c = (T)ca.c;
-    const bool ds_one = ds == (T)1;
-    long long *dep_acc = ca.dep_acc, *rad_acc = ca.rad_acc;
-    if (SMT) {
-        dep_acc = tally_smem(smem_raw, table_bytes(ca, sizeof(T)));
-        rad_acc = dep_acc + 3 * (size_t)ca.K * ca.nc;
-        for (int i = threadIdx.x; i < 6 * ca.K * ca.nc; i += blockDim.x) dep_acc[i] = 0;
-    }
-    const T dt = (T)sc->dt;
-    uint8_t *gate = smem_raw + table_bytes(ca, sizeof(T)) + (SMT ? 6 * 8 * ca.K * ca.nc : 0);
-    fill_table<T>(ca, tab, ds);
-    fill_gate<T>(ca, gate, ds, c, dt);
-    __syncthreads();
-    unsigned long long *ask_count = &sc->qcount[IN_Q ? 2 * round + 2 : 0];
-    const uint32_t stage = kStageResume + (uint32_t)round;
-    const int b_dep = sc->b_dep, b_rad = sc->b_rad, b_lost = sc->b_lost;
-    const unsigned step = sc->step;
-    const unsigned long long seed = ca.seed;
-    const long long cap = ca.seg_cap;
-    const bool reflect_r = ca.bc[1] == 1, reflect_l = ca.bc[0] == 1;
-    unsigned long long segs = 0, calls = 0;
-    unsigned flags = 0;
-    T emax = (T)0;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
-        Hist<T> h;
-        if (IN_Q) {
-            load_queued<T>(w.resume, e, seed, step, stage, h);
-        } else {
-            if (!pb.alive[e]) continue;
-            load_hist<St, T>(pb, tab, e, dt, seed, step, h);
-        }
-        const int res = walk_analog<T, SMT>(ca, tab, gate, h, PAUSE, c, ds, ds_one, dt, cap, N, reflect_l, reflect_r,
-                                            dep_acc, nc, b_dep, b_lost, flags, calls);
-        if (res == kPaused) store_queued<T>(w.ask, atomicAdd(ask_count, 1ull), h);
-        else if (res == kCensus) census<St, T, SMT>(pb, tab, h, rad_acc, nc, b_rad, flags, emax);
-        else pb.alive[h.i] = 0;
-        segs += (unsigned long long)h.seg;
-    }
-    if (SMT) flush_block_tallies(ca, dep_acc);
-    for (int off = 16; off > 0; off >>= 1) calls += __shfl_down_sync(kFull, calls, off);
-    if ((threadIdx.x & 31) == 0 && calls) atomicAdd(&sc->surrogate_calls, calls);
-    finish_counters<T>(sc, segs, flags, emax);
 }
 
 // ------------------------------------------------------------- query pass
@@ -538,23 +337,13 @@ __global__ void k_surr_image(const float *P, uint4 *dst) {
     for (int v = threadIdx.x; v < kImageBytes / 16; v += blockDim.x) dst[v] = src[v];
 }
 
-template <class St, int B, bool SMT>
-const void *analog_ptr(int which) {
-    if (which == 0) return (const void *)k_wave_analog<St, B, SMT, false, true>;
-    if (which == 1) return (const void *)k_wave_analog<St, B, SMT, true, true>;
-    return (const void *)k_wave_analog<St, B, SMT, true, false>;
-}
-
-template <class St, int B, bool SMT>
-void launch_wave(const CellArgs &ca, Scalars *sc, PBufPair bufs, const SurrWave &w, const SurrShapes &sh,
+template <class St>
+void launch_wave(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, const SurrWave &w, const SurrShapes &sh,
                  cudaStream_t st) {
-    k_wave_analog<St, B, SMT, false, true><<<sh.analog_grid, B, sh.analog_smem, st>>>(ca, sc, bufs, w, 0);
+    launch_surr_analog(ca, sc, prec, bufs, w, 0, 0, sh.analog_grid, sh.analog_smem, st);
     for (int r = 0; r < kSurrRounds; ++r) {
         k_wave_query<St><<<sh.query_grid, kQueryBlock, sh.query_smem, st>>>(ca, sc, bufs, w, r);
-        if (r + 1 < kSurrRounds)
-            k_wave_analog<St, B, SMT, true, true><<<sh.analog_grid, B, sh.analog_smem, st>>>(ca, sc, bufs, w, r);
-        else
-            k_wave_analog<St, B, SMT, true, false><<<sh.analog_grid, B, sh.analog_smem, st>>>(ca, sc, bufs, w, r);
+        launch_surr_analog(ca, sc, prec, bufs, w, r + 1 < kSurrRounds ? 1 : 2, r, sh.analog_grid, sh.analog_smem, st);
     }
 }
 
@@ -564,7 +353,7 @@ SurrShapes surr_shapes(const CellArgs &ca, int prec) {
     SurrShapes s{};
     const TransportShape ts = transport_shape(ca, prec);
     s.analog_block = ts.block;
-    s.analog_smem = ts.smem + ((ca.nx + 15) & ~15);  // + the per-cell gate
+    s.analog_smem = surr_analog_smem(ca, prec);
     s.analog_smt = ts.smem_tally;
     s.query_block = kQueryBlock;
     s.query_smem = kQueryHead + table_bytes(ca, 4);
@@ -572,21 +361,14 @@ SurrShapes surr_shapes(const CellArgs &ca, int prec) {
 }
 
 const void *surr_kernel_ptr(const CellArgs &ca, int prec, int which) {
-    const bool smt = transport_shape(ca, prec).smem_tally;
     if (which == 3) return prec == 2 ? (const void *)k_wave_query<StF16> : (const void *)k_wave_query<StF32>;
-    if (prec == 2) return smt ? analog_ptr<StF16, kSmtBlock32, true>(which) : analog_ptr<StF16, 256, false>(which);
-    return smt ? analog_ptr<StF32, kSmtBlock32, true>(which) : analog_ptr<StF32, 256, false>(which);
+    return surr_analog_ptr(ca, prec, which);
 }
 
 void launch_transport_surr(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, const SurrWave &w,
                            const SurrShapes &sh, cudaStream_t st) {
-    if (prec == 2) {
-        if (sh.analog_smt) launch_wave<StF16, kSmtBlock32, true>(ca, sc, bufs, w, sh, st);
-        else launch_wave<StF16, 256, false>(ca, sc, bufs, w, sh, st);
-    } else {
-        if (sh.analog_smt) launch_wave<StF32, kSmtBlock32, true>(ca, sc, bufs, w, sh, st);
-        else launch_wave<StF32, 256, false>(ca, sc, bufs, w, sh, st);
-    }
+    if (prec == 2) launch_wave<StF16>(ca, sc, prec, bufs, w, sh, st);
+    else launch_wave<StF32>(ca, sc, prec, bufs, w, sh, st);
 }
 
 void launch_surr_image(const float *params, void *dst, cudaStream_t st) {
