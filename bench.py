@@ -22,6 +22,9 @@ One bench step is one full simulation (t = 0 -> 3).  Printed on one JSON line:
                plain FP64, relerr against tests/golden/thick_fp64_mean.npz
   c3           the nonlinear heat wave, FP32 state against plain FP64,
                relerr against tests/golden/c3_fp64_mean.npz
+  c5           the 256-deck batched ensemble (tests/golden/c5_decks.py) run
+               side by side: learned + FP32 and plain FP32 throughput over all
+               decks, per-deck error and FOM against plain FP64 on 16 decks
   e2e          segments/s through the public API with host buffers: deck
                upload, run and the read-back of the cell fields per step
   roofline     the transport kernel: algorithmic bytes per launch over its
@@ -263,6 +266,69 @@ def c3_section(n):
             "fom_ratio_fp32_over_fp64": fp32["fom"] / fp64["fom"]}
 
 
+def c5_section(n_err=16):
+    """The batched ensemble (256 1D decks of tests/golden/c5_decks.py) run
+    side by side with imc_run_batch: learned surrogate + FP32 state and plain
+    FP32 state over all 256 decks (throughput), and per-deck temperature error
+    on the first n_err decks: learned+FP32 and plain FP64 runs (seeds + 1000)
+    against plain FP64 runs of other seeds (seeds + 2000)."""
+    import numpy as np
+    import mpimc
+    from mpimc import surrogate
+    sys.path.insert(0, GOLDEN)
+    from c5_decks import c5_decks
+
+    P = surrogate.train()
+
+    def batch(n, seed_offset, overrides=None, params=None):
+        engines = [mpimc.Engine(i, m, overrides) for i, m in c5_decks(n, seed_offset=seed_offset)]
+        try:
+            if params is not None:
+                for e in engines:
+                    e.set_surrogate(params)
+            steps, wall = mpimc.run_batch(engines, threads=16)
+            tot = np.array([e.totals() for e in engines], dtype=np.float64)
+            temps = [e.field("temp") for e in engines]
+        finally:
+            for e in engines:
+                e.close()
+        return {"wall_s": wall, "steps": int(sum(steps)), "segments": float(tot[:, 0].sum()),
+                "histories": float(tot[:, 1].sum()), "surrogate_calls": float(tot[:, 2].sum()), "temp": temps}
+
+    fp64 = {"precision": 0, "scale_select_precision": 0}
+    learned = batch(256, 0, None, P)
+    plain = batch(256, 0)
+    ref = batch(n_err, 2000, fp64)
+    l_err = batch(n_err, 1000, None, P)
+    f_err = batch(n_err, 1000, fp64)
+
+    def rel(run):
+        r = []
+        for a, b in zip(run["temp"], ref["temp"]):
+            live = b > 0.02
+            r.append(float(np.sqrt(np.mean(((a[live] - b[live]) / b[live]) ** 2))) if live.any() else 0.0)
+        return r
+
+    rl, rf = rel(l_err), rel(f_err)
+    rms_l, rms_f = float(np.sqrt(np.mean(np.square(rl)))), float(np.sqrt(np.mean(np.square(rf))))
+    fom_l = 1.0 / (rms_l ** 2 * l_err["wall_s"])
+    fom_f = 1.0 / (rms_f ** 2 * f_err["wall_s"])
+    return {"decks": 256, "workload": "256 1D decks: cells log-uniform 50-2000, sigma_a log-uniform 0.1-1000 with "
+                                      "power 0 or -3, bee 0.05-1, left surface T 0.2-1, NINPUT 1e4-1e6, RAMP to t=1",
+            "learned_fp32": {"wall_s": learned["wall_s"], "segments_per_s": learned["segments"] / learned["wall_s"],
+                             "histories_per_s": learned["histories"] / learned["wall_s"],
+                             "surrogate_calls": learned["surrogate_calls"], "segments": learned["segments"]},
+            "fp32": {"wall_s": plain["wall_s"], "segments_per_s": plain["segments"] / plain["wall_s"],
+                     "histories_per_s": plain["histories"] / plain["wall_s"], "segments": plain["segments"]},
+            "error_decks": n_err,
+            "relerr_T_learned_fp32": {"rms": rms_l, "median": float(np.median(rl)), "max": float(np.max(rl)),
+                                      "wall_s": l_err["wall_s"]},
+            "relerr_T_fp64": {"rms": rms_f, "median": float(np.median(rf)), "max": float(np.max(rf)),
+                              "wall_s": f_err["wall_s"]},
+            "fom_ratio_learned_over_fp64": fom_l / fom_f,
+            "error_reference": "plain FP64 runs of the same decks with other seeds (both arms carry its noise)"}
+
+
 def e2e_once(seed_offset):
     """Public-API run with host buffers: build the deck on the host, create the
     engine (uploads it), run, read the cell fields back, destroy."""
@@ -356,6 +422,7 @@ def main():
     ap.add_argument("--deck", default="c2", choices=sorted(DECKS), help="workload (c2 is the headline)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-surrogate comparison (thick slab)")
     ap.add_argument("--no-c3", action="store_true", help="skip the nonlinear heat-wave FP32 / FP64 comparison")
+    ap.add_argument("--no-c5", action="store_true", help="skip the 256-deck batched ensemble")
     ap.add_argument("--profile", action="store_true",
                     help="profiling case for ncu: the deck at half the particle counts, 12 timesteps, then exit")
     args = ap.parse_args()
@@ -464,6 +531,8 @@ def main():
         out["learned"] = learned_section(max(args.steps, 4))
     if not args.no_c3:
         out["c3"] = c3_section(2)
+    if not args.no_c5:
+        out["c5"] = c5_section()
     w, s, h2d, d2h = e2e_once(2000)
     out["e2e"] = {"value": s / w, "unit": "segments/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                   "wall_s_per_step": w}

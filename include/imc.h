@@ -229,6 +229,17 @@ int imc_run(ImcHandle *h, int64_t max_steps, ImcStepStats *stats,
 int imc_run_batch(ImcHandle *const *hs, int32_t n, int64_t max_steps, int32_t n_threads, int64_t *steps,
                   double *wall_ms, int32_t *failed);
 
+/* Checkpoint / resume.  imc_save_state copies the whole simulation state --
+ * clock, device scalars (energy balance, fixed-point ranges), cell fields and
+ * the particle list in its storage types -- into a host buffer: with buf
+ * NULL it sets *len to the size needed; otherwise *len is the buffer size on
+ * input and the size written on return.  imc_load_state restores such a blob
+ * into a handle created from the same deck (precision, geometry, mesh and
+ * scales must match); the run then continues exactly as the saved one would
+ * have (every random stream is keyed by the step index, which is restored). */
+int imc_save_state(const ImcHandle *h, void *buf, size_t *len);
+int imc_load_state(ImcHandle *h, const void *buf, size_t len);
+
 /* Totals over every step run by imc_step / imc_run since imc_create:
  * segments, histories (census carried in + births, per step) and surrogate
  * queries; any pointer may be NULL. */

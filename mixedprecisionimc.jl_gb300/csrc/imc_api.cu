@@ -941,6 +941,104 @@ int imc_set_field(ImcHandle *h, int field, const double *in, int64_t count) {
     return IMC_OK;
 }
 
+namespace {
+// layout of a state blob (imc_save_state): header, host clock and totals,
+// the device Scalars, the cell arrays, then the particle list's fields in
+// their storage types (buffer Scalars::cur)
+struct StateHeader {
+    char magic[8];
+    int32_t version, prec, geometry, nx, ny, K;
+    int64_t n_particles;
+    double t, dt;
+    int64_t step, finished, tot_segments, tot_histories, tot_calls;
+};
+constexpr int32_t kStateVersion = 1;
+
+struct Piece {
+    void *dev;
+    size_t bytes;
+};
+
+std::vector<Piece> cell_pieces(const ImcHandle *h) {
+    const size_t nc = (size_t)h->nc, nk = (size_t)h->nc * h->K;
+    const CellArgs &c = h->ca;
+    return {{c.temp, 8 * nc}, {c.bee, 8 * nc}, {c.beta, 8 * nc}, {c.fleck, 8 * nc}, {c.sa, 8 * nc}, {c.ss, 8 * nc},
+            {c.radenergydens, 8 * nc}, {c.matenergydens, 8 * nc}, {c.energydep, 8 * nk}, {c.emitted, 8 * nk}};
+}
+
+std::vector<Piece> particle_pieces(const ImcHandle *h, const PBufRaw &b, long long n) {
+    const size_t se = state_elem(h->prec), e0 = e0_elem(h->prec), m = (size_t)n;
+    std::vector<Piece> v = {{b.t, se * m}, {b.x, se * m}, {b.ux, se * m}, {b.E, se * m}, {b.E0, e0 * m},
+                            {b.cs, 4 * m}, {b.alive, m}};
+    if (h->geometry == 2) {
+        v.push_back({b.y, se * m});
+        v.push_back({b.uy, se * m});
+    }
+    return v;
+}
+}  // namespace
+
+int imc_save_state(const ImcHandle *hc, void *buf, size_t *len) {
+    if (!hc || !len) return IMC_ERR_INVALID_ARG;
+    ImcHandle *h = const_cast<ImcHandle *>(hc);
+    Scalars sc;
+    int rc = read_scalars(h, &sc);
+    if (rc) return rc;
+    const long long n = sc.n_particles;
+    auto cells = cell_pieces(h);
+    auto parts = particle_pieces(h, h->buf[sc.cur], n);
+    size_t need = sizeof(StateHeader) + sizeof(Scalars);
+    for (auto &p : cells) need += p.bytes;
+    for (auto &p : parts) need += p.bytes;
+    if (!buf) { *len = need; return IMC_OK; }
+    if (*len < need) { *len = need; return fail(h, IMC_ERR_INVALID_ARG, "state buffer too small"); }
+    unsigned char *o = static_cast<unsigned char *>(buf);
+    StateHeader hd{};
+    std::memcpy(hd.magic, "IMCSTATE", 8);
+    hd.version = kStateVersion; hd.prec = h->prec; hd.geometry = h->geometry; hd.nx = h->nx; hd.ny = h->ny; hd.K = h->K;
+    hd.n_particles = n; hd.t = h->t; hd.dt = h->dt; hd.step = h->step; hd.finished = h->finished ? 1 : 0;
+    hd.tot_segments = h->tot_segments; hd.tot_histories = h->tot_histories; hd.tot_calls = h->tot_calls;
+    std::memcpy(o, &hd, sizeof hd); o += sizeof hd;
+    std::memcpy(o, &sc, sizeof sc); o += sizeof sc;
+    for (auto &p : cells) { CK(h, hcopy(h, o, p.dev, p.bytes, cudaMemcpyDeviceToHost)); o += p.bytes; }
+    for (auto &p : parts) { if (p.bytes) CK(h, hcopy(h, o, p.dev, p.bytes, cudaMemcpyDeviceToHost)); o += p.bytes; }
+    *len = need;
+    return IMC_OK;
+}
+
+int imc_load_state(ImcHandle *h, const void *buf, size_t len) {
+    if (!h || !buf || len < sizeof(StateHeader) + sizeof(Scalars)) return IMC_ERR_INVALID_ARG;
+    const unsigned char *in = static_cast<const unsigned char *>(buf);
+    StateHeader hd;
+    std::memcpy(&hd, in, sizeof hd); in += sizeof hd;
+    if (std::memcmp(hd.magic, "IMCSTATE", 8) != 0 || hd.version != kStateVersion)
+        return fail(h, IMC_ERR_INVALID_ARG, "not a state blob of this library version");
+    if (hd.prec != h->prec || hd.geometry != h->geometry || hd.nx != h->nx || hd.ny != h->ny || hd.K != h->K)
+        return fail(h, IMC_ERR_INVALID_ARG, "state blob of another deck (precision, geometry, mesh or scales)");
+    Scalars sc;
+    std::memcpy(&sc, in, sizeof sc); in += sizeof sc;
+    const long long n = hd.n_particles;
+    int rc = grow(h, n);
+    if (rc) return rc;
+    auto cells = cell_pieces(h);
+    auto parts = particle_pieces(h, h->buf[0], n);
+    size_t need = sizeof(StateHeader) + sizeof(Scalars);
+    for (auto &p : cells) need += p.bytes;
+    for (auto &p : parts) need += p.bytes;
+    if (len < need) return fail(h, IMC_ERR_INVALID_ARG, "state blob truncated");
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (auto &p : cells) { CK(h, hcopy(h, p.dev, in, p.bytes, cudaMemcpyHostToDevice)); in += p.bytes; }
+    for (auto &p : parts) { if (p.bytes) CK(h, hcopy(h, p.dev, in, p.bytes, cudaMemcpyHostToDevice)); in += p.bytes; }
+    sc.cur = 0;
+    sc.compact_src = 0;
+    CK(h, hcopy(h, h->d_sc, &sc, sizeof sc, cudaMemcpyHostToDevice));
+    h->t = hd.t; h->dt = hd.dt; h->step = hd.step; h->finished = hd.finished != 0;
+    h->tot_segments = hd.tot_segments; h->tot_histories = hd.tot_histories; h->tot_calls = hd.tot_calls;
+    h->stage = Stage::Fresh;
+    drop_graphs(h);
+    return IMC_OK;
+}
+
 int imc_get_particles(const ImcHandle *hc, ImcParticles *p) {
     ImcHandle *h = const_cast<ImcHandle *>(hc);
     if (!h || !p) return IMC_ERR_INVALID_ARG;

@@ -156,6 +156,8 @@ SIGNATURES = {
     "imc_surrogate_sample": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
     "imc_set_surrogate": (C.c_int, [_H, C.c_void_p, C.c_int64]),
+    "imc_save_state": (C.c_int, [_H, C.c_void_p, C.POINTER(C.c_size_t)]),
+    "imc_load_state": (C.c_int, [_H, C.c_void_p, C.c_size_t]),
     "imc_get_totals": (C.c_int, [_H, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "imc_run_batch": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_int64, C.c_int32, C.POINTER(C.c_int64),
                                 C.POINTER(C.c_double), C.POINTER(C.c_int32)]),

@@ -273,6 +273,19 @@ class Engine:
         self._c(self.lib.imc_get_stats(self.h, C.byref(st)))
         return st.as_dict()
 
+    def save_state(self):
+        """The whole simulation state as bytes (imc_save_state)."""
+        n = C.c_size_t(0)
+        self._c(self.lib.imc_save_state(self.h, None, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        self._c(self.lib.imc_save_state(self.h, C.cast(buf, C.c_void_p), C.byref(n)))
+        return buf.raw[:n.value]
+
+    def load_state(self, blob):
+        """Restores a state saved from an Engine of the same deck."""
+        b = C.create_string_buffer(bytes(blob), len(blob))
+        self._c(self.lib.imc_load_state(self.h, C.cast(b, C.c_void_p), len(blob)))
+
     def totals(self):
         """(segments, histories, surrogate calls) over every step run so far."""
         a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
