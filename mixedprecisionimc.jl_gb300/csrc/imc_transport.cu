@@ -369,154 +369,230 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
     unsigned flags = 0;
     T emax = (T)0;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        if (!pb.alive[i]) continue;
-        const int cs = pb.cs[i];
+    // Lane state of the history in flight.
+    long long i = 0;
+    int cs = 0, xi = 0, yi = 0, k = 0, acc_cell = 0;
+    T t = (T)0, xp = (T)0, yp = (T)0, vx = (T)0, vy = (T)0, E = (T)0, E0 = (T)0, minenergy = (T)0;
+    T acc_s = (T)0, acc_c = (T)0;
+    long long seg = 0;
+    Stream rs;
+    auto start = [&]() {
         const int cell0 = cs & 0xFFFFFF;
-        const int k = cs >> 24;
-        int xi = cell0 % NX, yi = cell0 / NX;
-        T t, xp, yp, vx, vy, E, E0;
-        E0 = (T)pb.E0[i];
-        if (St::half) {
-            t = ld_f(pb.t + i) * (float)dtT;
-            xp = ld_f(pb.x + i) * (float)fx[xi].ws;
-            yp = ld_f(pb.y + i) * (float)fy[yi].ws;
-            vx = ld_f(pb.ux + i);
-            vy = ld_f(pb.uy + i);
-            E = ld_f(pb.E + i) * (float)E0;
-        } else {
-            t = (T)pb.t[i]; xp = (T)pb.x[i]; yp = (T)pb.y[i];
-            vx = (T)pb.ux[i]; vy = (T)pb.uy[i]; E = (T)pb.E[i];
-        }
-        Stream rs;
+        k = cs >> 24;
+        xi = cell0 % NX;
+        yi = cell0 / NX;
         rs.init(seed, step, (uint32_t)i, kStageTransport);
-        const T minenergy = (T)(0.01 * (double)E0);
-        T acc_s = (T)0, acc_c = (T)0;
-        int acc_cell = cell0;
-        bool alive = true;
-        long long seg = 0;
+        minenergy = (T)(0.01 * (double)E0);
+        acc_s = (T)0;
+        acc_c = (T)0;
+        acc_cell = cell0;
+        seg = 0;
+    };
+    auto load = [&](long long e, int &lcs, T &lt, T &lx, T &ly, T &lvx, T &lvy, T &lE, T &lE0) -> bool {
+        if (!pb.alive[e]) return false;
+        lcs = pb.cs[e];
+        const int c0 = lcs & 0xFFFFFF;
+        lE0 = (T)pb.E0[e];
+        if (St::half) {
+            lt = ld_f(pb.t + e) * (float)dtT;
+            lx = ld_f(pb.x + e) * (float)fx[c0 % NX].ws;
+            ly = ld_f(pb.y + e) * (float)fy[c0 / NX].ws;
+            lvx = ld_f(pb.ux + e);
+            lvy = ld_f(pb.uy + e);
+            lE = ld_f(pb.E + e) * (float)lE0;
+        } else {
+            lt = (T)pb.t[e]; lx = (T)pb.x[e]; ly = (T)pb.y[e];
+            lvx = (T)pb.ux[e]; lvy = (T)pb.uy[e]; lE = (T)pb.E[e];
+        }
+        return true;
+    };
+    // one pass of the reference's while loop (src/imc_transport.jl:533-717);
+    // 0 = go on, 1 = killed or escaped, 2 = census
+    auto segment = [&]() -> int {
+        if (++seg > cap) { flags |= (1u << 2); return 1; }
+        const T dist_bx = vx > (T)0 ? m_abs((fx[xi].ws - xp) / vx) : m_abs(xp / vx);
+        const T dist_by = vy > (T)0 ? m_abs((fy[yi].ws - yp) / vy) : m_abs(yp / vy);
+        T dist_b;
+        if (dist_bx != dist_bx) dist_b = dist_by;
+        else if (dist_by != dist_by) dist_b = dist_bx;
+        else dist_b = jmin(dist_bx, dist_by);
+        const int cell = xi + yi * NX;
+        const Tab2<T> ce = tab[cell];
+        T dist_col, Edens, newenergy, dep;
+        if constexpr (sizeof(T) == 4) {
+            // FP32: the 1D kernels' formulation (SegMath<float>)
+            const float v = (float)((rs.next() >> 8) | 1u) * 0x1p-24f;
+            dist_col = -__logf(v) * ce.rseff;
+        } else {
+            dist_col = Rand<T>::exp1(rs) / ce.seff;
+        }
+        const T dist_cen = c * (dtT - t) * ds;
+        const T dist = jmin(jmin(dist_b, dist_col), dist_cen);
+        if (dist != dist) { flags |= 1u; return 1; }
+        if constexpr (sizeof(T) == 4) {
+            const float em1 = expm1f(-ce.saf * dist);
+            newenergy = E + E * em1;
+            Edens = E * ce.rarea;
+            dep = -Edens * em1;
+        } else {
+            newenergy = E * m_exp(-ce.saf * dist);
+            Edens = (E / fx[xi].wT) / fy[yi].wT;
+            dep = -Edens * m_expm1(-ce.saf * dist);
+        }
+        if (cell != acc_cell) {
+            flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+            acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
+        }
+        if (newenergy <= minenergy) {
+            nadd(acc_s, acc_c, Edens);
+            return 1;
+        }
+        nadd(acc_s, acc_c, dep);
+        xp += dist * vx;
+        yp += dist * vy;
+        if constexpr (sizeof(T) == 4) t += dist * rdsc;
+        else t += (ds_one ? dist : dist / ds) / c;
+        E = newenergy;
+        if (dist == dist_bx || dist == dist_by) {
+            if (dist_bx < dist_by) {
+                if (vx > (T)0) {
+                    if (xi == NX - 1) {
+                        if (refl_r) { vx = -vx; return 0; }
+                        flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
+                        return 1;
+                    }
+                    xi += 1; xp = (T)0;
+                } else {
+                    if (xi == 0) {
+                        if (refl_l) { vx = -vx; return 0; }
+                        flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
+                        return 1;
+                    }
+                    xi -= 1; xp = fx[xi].ws;
+                }
+            } else {
+                if (vy > (T)0) {
+                    if (yi == NY - 1) {
+                        if (refl_t) { vy = -vy; return 0; }
+                        flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
+                        return 1;
+                    }
+                    yi += 1; yp = (T)0;
+                } else {
+                    if (yi == 0) {
+                        if (refl_b) { vy = -vy; return 0; }
+                        flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
+                        return 1;
+                    }
+                    yi -= 1; yp = fy[yi].ws;
+                }
+            }
+            return 0;
+        }
+        if (dist == dist_col) {
+            // isotropic re-emission: angle 2*pi*rand in Float64, rounded to T
+            // (FP32: the hardware sine and cosine)
+            T ang = (T)(6.283185307179586 * (double)Rand<T>::u(rs));
+            if constexpr (sizeof(T) == 4) __sincosf(ang, &vy, &vx);
+            else m_sincos(ang, &vy, &vx);
+        }
+        if (dist == dist_cen) {
+            const int cellf = xi + yi * NX;
+            T Est = E;
+            if (St::half) {
+                st_v(pb.t + i, 0.0f);
+                st_v(pb.x + i, (float)xp / (float)fx[xi].ws);
+                st_v(pb.y + i, (float)yp / (float)fy[yi].ws);
+                st_v(pb.ux + i, (float)vx);
+                st_v(pb.uy + i, (float)vy);
+                __half ef = __float2half_rn((float)E / (float)E0);
+                pb.E[i] = ef;
+                Est = __half2float(ef) * (float)E0;
+            } else {
+                pb.t[i] = (typename St::S)0;
+                pb.x[i] = (typename St::S)xp;
+                pb.y[i] = (typename St::S)yp;
+                pb.ux[i] = (typename St::S)vx;
+                pb.uy[i] = (typename St::S)vy;
+                pb.E[i] = (typename St::S)E;
+            }
+            if (cellf != (cs & 0xFFFFFF)) pb.cs[i] = cellf | (k << 24);
+            flush_one<T, SMT>(rad_acc, k * nc + cellf, Est, b_rad, flags);
+            emax = Est > emax ? Est : emax;
+            return 2;
+        }
+        return 0;
+    };
+    auto finish = [&](int end) {
+        flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+        if (end == 1) pb.alive[i] = 0;
+        segs += (unsigned long long)seg;
+    };
+    if (sc->seg_per_hist < kRefillSegments) {
+        // short histories: one history per lane to its end (see k_transport1d)
+        for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+            if (!load(e, cs, t, xp, yp, vx, vy, E, E0)) continue;
+            i = e;
+            start();
+            int end;
+            do end = segment(); while (!end);
+            finish(end);
+        }
+    } else {
+        // long histories: lanes refill from 32-entry chunks (see k_transport1d)
+        const int lane = threadIdx.x & 31;
+        const unsigned lt = (1u << lane) - 1u;
+        const long long nchunks = (n + 31) / 32;
+        const long long cstride = (long long)gridDim.x * (BLOCK / 32);
+        long long chunk = (long long)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
+        int p_cs = -1;
+        T p_t = (T)0, p_x = (T)0, p_y = (T)0, p_vx = (T)0, p_vy = (T)0, p_E = (T)0, p_E0 = (T)0;
+        auto prefetch = [&]() {
+            const long long e = chunk * 32 + lane;
+            int lcs = -1;
+            if (!(e < n && load(e, lcs, p_t, p_x, p_y, p_vx, p_vy, p_E, p_E0))) lcs = -1;
+            p_cs = lcs;
+        };
+        bool more = chunk < nchunks;
+        int pos = 0;
+        if (more) prefetch();
+        bool has = false;
         while (true) {
-            if (++seg > cap) { flags |= (1u << 2); alive = false; break; }
-            T dist_bx = vx > (T)0 ? m_abs((fx[xi].ws - xp) / vx) : m_abs(xp / vx);
-            T dist_by = vy > (T)0 ? m_abs((fy[yi].ws - yp) / vy) : m_abs(yp / vy);
-            T dist_b;
-            if (dist_bx != dist_bx) dist_b = dist_by;
-            else if (dist_by != dist_by) dist_b = dist_bx;
-            else dist_b = jmin(dist_bx, dist_by);
-            const int cell = xi + yi * NX;
-            const Tab2<T> ce = tab[cell];
-            T dist_col, Edens, newenergy, dep;
-            if constexpr (sizeof(T) == 4) {
-                // FP32: the 1D kernels' formulation (SegMath<float>)
-                const float v = (float)((rs.next() >> 8) | 1u) * 0x1p-24f;
-                dist_col = -__logf(v) * ce.rseff;
-            } else {
-                dist_col = Rand<T>::exp1(rs) / ce.seff;
-            }
-            T dist_cen = c * (dtT - t) * ds;
-            T dist = jmin(jmin(dist_b, dist_col), dist_cen);
-            if (dist != dist) { flags |= 1u; alive = false; break; }
-            if constexpr (sizeof(T) == 4) {
-                const float em1 = expm1f(-ce.saf * dist);
-                newenergy = E + E * em1;
-                Edens = E * ce.rarea;
-                dep = -Edens * em1;
-            } else {
-                newenergy = E * m_exp(-ce.saf * dist);
-                Edens = (E / fx[xi].wT) / fy[yi].wT;
-                dep = -Edens * m_expm1(-ce.saf * dist);
-            }
-            if (cell != acc_cell) {
-                flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
-                acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
-            }
-            if (newenergy <= minenergy) {
-                nadd(acc_s, acc_c, Edens);
-                alive = false;
-                break;
-            }
-            nadd(acc_s, acc_c, dep);
-            xp += dist * vx;
-            yp += dist * vy;
-            if constexpr (sizeof(T) == 4) t += dist * rdsc;
-            else t += (ds_one ? dist : dist / ds) / c;
-            E = newenergy;
-            if (dist == dist_bx || dist == dist_by) {
-                if (dist_bx < dist_by) {
-                    if (vx > (T)0) {
-                        if (xi == NX - 1) {
-                            if (refl_r) { vx = -vx; continue; }
-                            flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
-                            alive = false;
-                            break;
-                        }
-                        xi += 1; xp = (T)0;
-                    } else {
-                        if (xi == 0) {
-                            if (refl_l) { vx = -vx; continue; }
-                            flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
-                            alive = false;
-                            break;
-                        }
-                        xi -= 1; xp = fx[xi].ws;
-                    }
-                } else {
-                    if (vy > (T)0) {
-                        if (yi == NY - 1) {
-                            if (refl_t) { vy = -vy; continue; }
-                            flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
-                            alive = false;
-                            break;
-                        }
-                        yi += 1; yp = (T)0;
-                    } else {
-                        if (yi == 0) {
-                            if (refl_b) { vy = -vy; continue; }
-                            flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
-                            alive = false;
-                            break;
-                        }
-                        yi -= 1; yp = fy[yi].ws;
-                    }
+            unsigned idle = __ballot_sync(0xFFFFFFFFu, !has);
+            while (idle && more) {
+                const int r = __popc(idle & lt);
+                const int avail = 32 - pos;
+                const int sl = (pos + r) & 31;
+                const int q_cs = __shfl_sync(0xFFFFFFFFu, p_cs, sl);
+                const T q_t = __shfl_sync(0xFFFFFFFFu, p_t, sl), q_x = __shfl_sync(0xFFFFFFFFu, p_x, sl);
+                const T q_y = __shfl_sync(0xFFFFFFFFu, p_y, sl), q_vx = __shfl_sync(0xFFFFFFFFu, p_vx, sl);
+                const T q_vy = __shfl_sync(0xFFFFFFFFu, p_vy, sl), q_E = __shfl_sync(0xFFFFFFFFu, p_E, sl);
+                const T q_E0 = __shfl_sync(0xFFFFFFFFu, p_E0, sl);
+                if (!has && r < avail && q_cs >= 0) {
+                    i = chunk * 32 + pos + r;
+                    cs = q_cs;
+                    t = q_t; xp = q_x; yp = q_y; vx = q_vx; vy = q_vy; E = q_E; E0 = q_E0;
+                    start();
+                    has = true;
                 }
-                continue;
-            }
-            if (dist == dist_col) {
-                // isotropic re-emission: angle 2*pi*rand in Float64, rounded to T
-                // (FP32: the hardware sine and cosine)
-                T ang = (T)(6.283185307179586 * (double)Rand<T>::u(rs));
-                if constexpr (sizeof(T) == 4) __sincosf(ang, &vy, &vx);
-                else m_sincos(ang, &vy, &vx);
-            }
-            if (dist == dist_cen) {
-                const int cellf = xi + yi * NX;
-                T Est = E;
-                if (St::half) {
-                    st_v(pb.t + i, 0.0f);
-                    st_v(pb.x + i, (float)xp / (float)fx[xi].ws);
-                    st_v(pb.y + i, (float)yp / (float)fy[yi].ws);
-                    st_v(pb.ux + i, (float)vx);
-                    st_v(pb.uy + i, (float)vy);
-                    __half ef = __float2half_rn((float)E / (float)E0);
-                    pb.E[i] = ef;
-                    Est = __half2float(ef) * (float)E0;
-                } else {
-                    pb.t[i] = (typename St::S)0;
-                    pb.x[i] = (typename St::S)xp;
-                    pb.y[i] = (typename St::S)yp;
-                    pb.ux[i] = (typename St::S)vx;
-                    pb.uy[i] = (typename St::S)vy;
-                    pb.E[i] = (typename St::S)E;
+                const int nidle = __popc(idle);
+                pos += nidle < avail ? nidle : avail;
+                if (pos >= 32) {
+                    chunk += cstride;
+                    more = chunk < nchunks;
+                    pos = 0;
+                    if (more) prefetch();
                 }
-                if (cellf != cell0) pb.cs[i] = cellf | (k << 24);
-                flush_one<T, SMT>(rad_acc, k * nc + cellf, Est, b_rad, flags);
-                emax = Est > emax ? Est : emax;
-                break;
+                idle = __ballot_sync(0xFFFFFFFFu, !has);
+            }
+            if (idle == 0xFFFFFFFFu) break;
+            if (!has) continue;
+            const int end = segment();
+            if (end) {
+                finish(end);
+                has = false;
             }
         }
-        flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
-        if (!alive) pb.alive[i] = 0;
-        segs += (unsigned long long)seg;
     }
     if (SMT) flush_block_tallies(ca, dep_acc);
     finish_counters<T>(sc, segs, flags, emax);
