@@ -415,6 +415,26 @@ def profile_case():
     return 0
 
 
+def profile_learned_case():
+    """The thick slab (tests/golden/decks/thick_slab.txt, 2e6 particles) with
+    the learned surrogate, 10 timesteps run as graphs; for ncu captures of the
+    query pass (k_wave_query) and the list / resume passes."""
+    import mpimc
+    from mpimc import _build, surrogate
+    _build.build()
+    P = surrogate.train()
+    inputs = mpimc.Input.readInputs(os.path.join(GOLDEN, "decks", "thick_slab.txt"))
+    mesh = mpimc.Mesh.mesh_generation(inputs)
+    eng = mpimc.Engine(inputs, mesh)
+    eng.set_surrogate(P)
+    steps, _ = eng.run(10)
+    print(json.dumps({"profile_case": "thick_slab+surrogate", "steps": len(steps),
+                      "segments": sum(s["segments"] for s in steps),
+                      "surrogate_calls": sum(s["surrogate_calls"] for s in steps)}))
+    eng.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -430,10 +450,14 @@ def main():
     ap.add_argument("--no-c5", action="store_true", help="skip the 256-deck batched ensemble")
     ap.add_argument("--profile", action="store_true",
                     help="profiling case for ncu: the deck at half the particle counts, 12 timesteps, then exit")
+    ap.add_argument("--profile-learned", action="store_true",
+                    help="profiling case for ncu: the thick slab with the learned surrogate, 10 timesteps, then exit")
     args = ap.parse_args()
     select_deck(args.deck)
     if args.profile:
         return profile_case()
+    if args.profile_learned:
+        return profile_learned_case()
     rank, world, local = _env_rank()
     if world > 1:
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))

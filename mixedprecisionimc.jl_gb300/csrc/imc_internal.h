@@ -23,7 +23,7 @@
 namespace imc {
 
 // query rounds per step of the surrogate transport (launch_transport_surr)
-constexpr int kSurrRounds = 1;  // measured best on GB300: each further round costs a pass whose tail outweighs its queries
+constexpr int kSurrRounds = 1;  // measured best on GB300 (thick slab: 1 round 84 ms, 3 rounds 104 ms, 6 rounds 134 ms)
 
 // scalars that live in device memory so a whole step can replay as a graph
 struct Scalars {

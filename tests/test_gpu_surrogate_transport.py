@@ -110,3 +110,22 @@ def test_main_with_randomwalk_uses_the_surrogate(tmp_path, surrogate_params):
     assert sum(s["surrogate_calls"] for s in res.steps) > 0
     plain = mpimc.main([deck_path("thick_slab")], verbose=False)
     assert sum(s["surrogate_calls"] for s in plain.steps) == 0
+
+
+def test_surrogate_with_fp16_state(surrogate_params):
+    """FP16 particle state with the surrogate: runs, conserves energy to the
+    FP32 arithmetic's level, queries the network, and is reproducible."""
+    import mpimc
+    P, _ = surrogate_params
+    out = []
+    for _ in range(2):
+        inputs, mesh = load_deck("thick_slab", SEED="31", NINPUT="20000", NMAX="200000")
+        e = mpimc.Engine(inputs, mesh, {"precision": 2, "scale_select_precision": 2})
+        e.set_surrogate(P)
+        steps, _ = e.run()
+        out.append(e.field("temp"))
+        assert sum(s["surrogate_calls"] for s in steps) > 0
+        for s in steps[:-1]:
+            assert abs(s["energy_error"]) < 1e-4 and s["error_flags"] == 0
+        e.close()
+    assert np.array_equal(out[0], out[1])
