@@ -118,17 +118,6 @@ __device__ __forceinline__ bool cross_face(const CellArgs &ca, const Tab1<T> *ta
     return true;
 }
 
-// the per-cell deposit accumulator follows the history's cell
-template <class T, bool SMT>
-__device__ __forceinline__ void follow_cell(Hist<T> &h, long long *dep_acc, int nc, int b_dep, unsigned &flags) {
-    if (h.cell != h.acc_cell) {
-        flush_pair<T, SMT>(dep_acc, h.k * nc + h.acc_cell, h.acc_s, h.acc_c, b_dep, flags);
-        h.acc_s = (T)0;
-        h.acc_c = (T)0;
-        h.acc_cell = h.cell;
-    }
-}
-
 enum { kGo = 0, kKilled = 1, kCensus = 2, kPaused = 3 };
 
 template <class T>
