@@ -97,6 +97,20 @@ for _p in (PKG, os.path.join(REPO, "oracle")):
         sys.path.insert(0, _p)
 
 
+def combine_ranks(dist, dev_ms, segs, hist):
+    """Replicas on N GPUs: the job's time is the slowest rank's, its work the
+    sum over ranks (no data-path collective; one reduction of three numbers).
+    Returns (max device ms, total segments, total histories)."""
+    if dist is None:
+        return dev_ms, segs, hist
+    import torch
+    tt = torch.tensor([dev_ms, segs, hist], dtype=torch.float64)
+    mx = tt.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(tt, op=dist.ReduceOp.SUM)
+    return float(mx[0]), float(tt[1]), float(tt[2])
+
+
 def _env_rank():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -488,14 +502,7 @@ def main():
     dev_ms = sum(r["ms"] for r in runs)
     segs = sum(r["segments"] for r in runs)
     hist = sum(r["histories"] for r in runs)
-    t_max = dev_ms
-    if dist:
-        import torch
-        tt = torch.tensor([dev_ms, segs, hist], dtype=torch.float64)
-        mx = tt.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        dist.all_reduce(tt, op=dist.ReduceOp.SUM)
-        t_max, segs, hist = float(mx[0]), float(tt[1]), float(tt[2])
+    t_max, segs, hist = combine_ranks(dist, dev_ms, segs, hist)
     if rank != 0:
         return 0
     value = segs / (t_max / 1000.0)
