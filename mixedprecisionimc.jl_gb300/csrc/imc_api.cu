@@ -537,8 +537,8 @@ int imc_create(const ImcDeck *d, ImcHandle **out) {
     if ((rc = upload<long long>(h, &ca.slot_n, nullptr, h->nslots))) return bail(rc);
     if ((rc = upload<long long>(h, &ca.slot_off, nullptr, h->nslots))) return bail(rc);
     if ((rc = upload<double>(h, &ca.slot_q, nullptr, h->nslots))) return bail(rc);
-    ca.nblk_slot = (h->nslots + 63) / 64;
-    ca.nblk_cell = (nc + 63) / 64;
+    ca.nblk_slot = (h->nslots + kCellThreads - 1) / kCellThreads;
+    ca.nblk_cell = (nc + kCellThreads - 1) / kCellThreads;
     if ((rc = upload<double>(h, &ca.part_src, nullptr, (size_t)ca.nblk_slot * 12))) return bail(rc);
     if ((rc = upload<double>(h, &ca.part_emax, nullptr, (size_t)ca.nblk_slot))) return bail(rc);
     if ((rc = upload<double>(h, &ca.part_tally, nullptr, (size_t)ca.nblk_cell * (K + 1) * 2))) return bail(rc);

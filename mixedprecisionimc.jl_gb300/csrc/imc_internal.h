@@ -40,6 +40,7 @@ struct Scalars {
     double n_source;                   // particle budget of this step
     unsigned long long segments;
     unsigned long long surrogate_calls;
+    unsigned long long killed;         // histories this transport removed (kill, escape, cap)
     float seg_per_hist;                // segments per history of the last transport
     unsigned long long qcount[2 * kSurrRounds + 1];  // surrogate transport: ask queue of round r at 2r, resume queue at 2r + 1
     unsigned int flags;
@@ -64,7 +65,7 @@ struct CellArgs {
     int *slot_j;
     long long *slot_n, *slot_off;
     // per-block partial sums (double-double pairs) and maxima
-    int nblk_slot, nblk_cell;          // 64-thread blocks over slots / cells
+    int nblk_slot, nblk_cell;          // kCellThreads-thread blocks over slots / cells
     double *part_src;                  // [nblk_slot][6 groups][hi, lo]
     double *part_emax;                 // [nblk_slot]
     double *part_tally;                // [nblk_cell][K + 1][hi, lo]
@@ -161,6 +162,10 @@ void launch_timestep(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 void launch_prepare_transport(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 const void *transport_kernel_ptr(const CellArgs &ca, int prec);
 
+// threads per block of the per-cell / per-slot FP64 kernels: one warp, so that
+// a 2000-cell mesh spreads over 63 SMs (FP64 runs at 1/64 of the FP32 rate,
+// and these kernels are latency bound)
+constexpr int kCellThreads = 32;
 constexpr int kCompactTile = 4096;     // particles per compaction tile
 constexpr int kCompactThreads = 256;
 

@@ -27,7 +27,6 @@ constexpr int kPlanThreads = 1024;
 // GB300 executes FP64 at 1/64 of the FP32 rate, so every per-cell FP64 stage
 // runs as many 64-thread blocks spread over all SMs; sums are double-double
 // per block over a fixed partition of the cells, combined in block order.
-constexpr int kCellThreads = 64;
 
 __device__ __forceinline__ DD block_reduce_dd(DD v, DD *sh) {
     sh[threadIdx.x] = v;
@@ -345,6 +344,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_source_scan(CellArgs ca, Scala
         sc->emax_census_bits = 0ull;
         sc->segments = 0ull;
         sc->surrogate_calls = 0ull;
+        sc->killed = 0ull;
         for (int r = 0; r <= 2 * kSurrRounds; ++r) sc->qcount[r] = 0ull;
         sc->b_dep = fix_exponent(emax / ca.vol_min);
         sc->b_lost = fix_exponent(emax);
@@ -504,14 +504,25 @@ void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufPair buf, int 
 // survivors in order into the other buffer.
 __global__ void __launch_bounds__(kCompactThreads) k_compact_count(const Scalars *sc, PBufPair bufs,
                                                                    long long *tile_cnt) {
+    if (!sc->compact_now) return;
     const uint8_t *alive = bufs.b[sc->cur].alive;
     const long long n = sc->n_particles;
     const long long base = (long long)blockIdx.x * kCompactTile;
     if (base >= n) return;
     int cnt = 0;
-    for (int r = threadIdx.x; r < kCompactTile; r += blockDim.x) {
-        long long i = base + r;
-        if (i < n && alive[i]) ++cnt;
+    if (base + kCompactTile <= n) {
+        // a full tile: 16 alive bytes per thread in one 16-byte load (tiles
+        // start at multiples of 4096 bytes, so every load is aligned)
+        static_assert(kCompactTile == 16 * kCompactThreads, "one uint4 per thread");
+        const uint4 v = reinterpret_cast<const uint4 *>(alive + base)[threadIdx.x];
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+        for (int q = 0; q < 4; ++q)
+            for (int b = 0; b < 4; ++b) cnt += ((w[q] >> (8 * b)) & 0xFFu) != 0u;
+    } else {
+        for (int r = threadIdx.x; r < kCompactTile; r += blockDim.x) {
+            long long i = base + r;
+            if (i < n && alive[i]) ++cnt;
+        }
     }
     cnt = __reduce_add_sync(0xFFFFFFFFu, (unsigned)cnt);
     __shared__ int wt[kCompactThreads / 32];
@@ -528,6 +539,7 @@ __global__ void __launch_bounds__(1024) k_compact_scan(Scalars *sc, const long l
                                                       int force) {
     __shared__ long long warp_tot[32];
     __shared__ long long s_run;
+    if (!sc->compact_now) return;  // k_compact_decide set the live count
     const long long n = sc->n_particles;
     const long long ntiles = (n + kCompactTile - 1) / kCompactTile;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -561,14 +573,11 @@ __global__ void __launch_bounds__(1024) k_compact_scan(Scalars *sc, const long l
     if (threadIdx.x == 0) {
         // compact when forced (Clean.clean) or when the holes exceed 1/16 of the list
         const long long alive = s_run;
-        const bool compact = force || (n - alive) * kDeferHoles > n;
+        (void)force;
         sc->n_census = alive;
-        sc->compact_now = compact ? 1 : 0;
-        if (compact) {
-            sc->compact_src = sc->cur;
-            sc->cur ^= 1;
-            sc->n_particles = alive;
-        }
+        sc->compact_src = sc->cur;
+        sc->cur ^= 1;
+        sc->n_particles = alive;
     }
 }
 
@@ -649,13 +658,24 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(int geometr
     for (int j = threadIdx.x; j < cnt; j += blockDim.x) dst.alive[out + j] = 1;
 }
 
-__global__ void k_copy_count(const Scalars *sc, long long *n_before) { *n_before = sc->n_particles; }
+// Before compaction: the list length (for the scatter) and whether this step
+// compacts.  The live count follows from the transport's kills (census
+// carried in + births - removed), so the holes are known without reading the
+// alive bytes; they are counted per tile only when the list is compacted.
+__global__ void k_compact_decide(Scalars *sc, long long *n_before, int force) {
+    const long long n = sc->n_particles;
+    *n_before = n;
+    const long long live = sc->n_census_in + sc->n_sourced - (long long)sc->killed;
+    const bool compact = force || (n - live) * kDeferHoles > n;
+    sc->compact_now = compact ? 1 : 0;
+    if (!compact) sc->n_census = live;
+}
 
 void launch_compact(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, long long *tile_cnt,
                     long long *tile_off, long long ntiles_cap, bool force, cudaStream_t st) {
     // tile_off has ntiles_cap + 1 entries; the last holds the pre-compaction length
     long long *n_before = tile_off + ntiles_cap;
-    k_copy_count<<<1, 1, 0, st>>>(sc, n_before);
+    k_compact_decide<<<1, 1, 0, st>>>(sc, n_before, force ? 1 : 0);
     k_compact_count<<<(unsigned)ntiles_cap, kCompactThreads, 0, st>>>(sc, bufs, tile_cnt);
     k_compact_scan<<<1, 1024, 0, st>>>(sc, tile_cnt, tile_off, force ? 1 : 0);
     if (prec == 0)
@@ -844,6 +864,7 @@ __global__ void k_prepare_transport(CellArgs ca, Scalars *sc) {
     sc->emax_census_bits = 0ull;
     sc->segments = 0ull;
     sc->surrogate_calls = 0ull;
+    sc->killed = 0ull;
     for (int r = 0; r <= 2 * kSurrRounds; ++r) sc->qcount[r] = 0ull;
     sc->n_census_in = sc->n_census;
     sc->n_sourced = 0;

@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     const bool reflect_r = ca.bc[1] == 1, reflect_l = ca.bc[0] == 1;
     unsigned long long *ask_count = &sc->qcount[kFromQueue ? 2 * round + 2 : 0];
     const uint32_t stage = kFromQueue ? kStageResume + (uint32_t)round : kStageTransport;
-    unsigned long long segs = 0, calls = 0;
+    unsigned long long segs = 0, calls = 0, killed = 0;
     unsigned flags = 0;
     T emax = (T)0;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -238,6 +238,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
             w.ask.E0[j] = (float)E0; w.ask.cs[j] = cell | (k << 24); w.ask.cs_list[j] = cs; w.ask.idx[j] = i;
         } else if (end == 1) {
             pb.alive[i] = 0;
+            ++killed;
         }
         segs += (unsigned long long)seg;
     };
@@ -323,7 +324,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         for (int off = 16; off > 0; off >>= 1) calls += __shfl_down_sync(0xFFFFFFFFu, calls, off);
         if (lane == 0 && calls) atomicAdd(&sc->surrogate_calls, calls);
     }
-    finish_counters<T>(sc, segs, flags, emax);
+    finish_counters<T>(sc, segs, killed, flags, emax);
 }
 
 template <class St, int BLOCK, bool SMT>
@@ -365,7 +366,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
     const unsigned long long seed = ca.seed;
     const long long cap = ca.seg_cap;
     const bool refl_l = ca.bc[0] == 1, refl_r = ca.bc[1] == 1, refl_t = ca.bc[2] == 1, refl_b = ca.bc[3] == 1;
-    unsigned long long segs = 0;
+    unsigned long long segs = 0, killed = 0;
     unsigned flags = 0;
     T emax = (T)0;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -525,7 +526,10 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
     };
     auto finish = [&](int end) {
         flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
-        if (end == 1) pb.alive[i] = 0;
+        if (end == 1) {
+            pb.alive[i] = 0;
+            ++killed;
+        }
         segs += (unsigned long long)seg;
     };
     if (sc->seg_per_hist < kRefillSegments) {
@@ -595,7 +599,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
         }
     }
     if (SMT) flush_block_tallies(ca, dep_acc);
-    finish_counters<T>(sc, segs, flags, emax);
+    finish_counters<T>(sc, segs, killed, flags, emax);
 }
 
 // Launch shape of the transport kernel.  When the table and the block's

@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scal
     const unsigned long long seed = ca.seed;
     const long long cap = ca.seg_cap;
     const bool reflect_r = ca.bc[1] == 1, reflect_l = ca.bc[0] == 1;
-    unsigned long long calls = 0;
+    unsigned long long calls = 0, killed = 0;
     unsigned flags = 0;
     T emax = (T)0;
     const long long wstride = (long long)gridDim.x * kQueryWarps * 32;
@@ -297,7 +297,10 @@ __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scal
             }
             flush_pair<T, false>(ca.dep_acc, h.k * nc + h.acc_cell, h.acc_s, h.acc_c, b_dep, flags);
             if (res == kCensus) census<St, T, false>(pb, tab, h, ca.rad_acc, nc, b_rad, flags, emax);
-            else if (res == kKilled) pb.alive[h.i] = 0;
+            else if (res == kKilled) {
+                pb.alive[h.i] = 0;
+                ++killed;
+            }
         }
         // continuing histories go to the resume queue, one atomic per warp
         const bool go = valid && res == kGo;
@@ -312,7 +315,7 @@ __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scal
     }
     for (int off = 16; off > 0; off >>= 1) calls += __shfl_down_sync(kFull, calls, off);
     if (lane == 0 && calls) atomicAdd(&sc->surrogate_calls, calls);
-    finish_counters<T>(sc, 0ull, flags, emax);
+    finish_counters<T>(sc, 0ull, killed, flags, emax);
 }
 
 // BF16 fragment image of FP32 parameters (one block)
