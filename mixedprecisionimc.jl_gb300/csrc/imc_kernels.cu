@@ -25,8 +25,9 @@ namespace imc {
 constexpr int kPlanThreads = 1024;
 
 // GB300 executes FP64 at 1/64 of the FP32 rate, so every per-cell FP64 stage
-// runs as many 64-thread blocks spread over all SMs; sums are double-double
-// per block over a fixed partition of the cells, combined in block order.
+// runs as many one-warp blocks (kCellThreads) spread over the SMs; sums are
+// double-double per block over a fixed partition of the cells, combined in
+// block order.
 
 __device__ __forceinline__ DD block_reduce_dd(DD v, DD *sh) {
     sh[threadIdx.x] = v;
@@ -324,6 +325,16 @@ __global__ void __launch_bounds__(kPlanThreads) k_source_scan(CellArgs ca, Scala
         if (threadIdx.x == blockDim.x - 1) s_run = excl + v;
         __syncthreads();
     }
+    // largest birth energy over the per-block maxima, one warp wide (the
+    // loads are independent; a single thread would wait for each in turn)
+    __shared__ double s_emax;
+    if (warp == 0) {
+        double m = 0.0;
+        for (int bb = lane; bb < ca.nblk_slot; bb += 32) m = fmax(m, ca.part_emax[bb]);
+        for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_down_sync(0xFFFFFFFFu, m, off));
+        if (lane == 0) s_emax = m;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
         const long long n_census = sc->n_census;  // live particles
         const long long len = sc->n_particles;    // list length, holes included
@@ -334,8 +345,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_source_scan(CellArgs ca, Scala
             if (n_new < 0) n_new = 0;
             fl |= 1u << 3;
         }
-        double emax = __longlong_as_double((long long)sc->emax_census_bits);
-        for (int bb = 0; bb < ca.nblk_slot; ++bb) emax = fmax(emax, ca.part_emax[bb]);
+        const double emax = fmax(__longlong_as_double((long long)sc->emax_census_bits), s_emax);
         sc->n_census_in = n_census;
         sc->n_sourced = n_new;
         sc->birth_base = len;
