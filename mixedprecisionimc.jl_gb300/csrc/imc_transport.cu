@@ -606,7 +606,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
 // private tallies fit in shared memory the kernel runs one large block per
 // SM with shared tallies (kSmtBlock32 threads for FP32 / FP16 state,
 // kSmtBlock64 for FP64);
-// otherwise 256-thread blocks with tallies in global memory.
+// otherwise tallies in global memory (kGlbBlock32 / kGlbBlock64 threads).
 constexpr int kSmemBudget = 200 * 1024;
 
 TransportShape transport_shape(const CellArgs &ca, int prec) {
@@ -616,7 +616,7 @@ TransportShape transport_shape(const CellArgs &ca, int prec) {
     const long long tallies = 2ll * 3 * 8 * (long long)ca.K * ca.nc;
     sh.smem_tally = table + tallies <= kSmemBudget;
     sh.smem = sh.smem_tally ? (int)(table + tallies) : table;
-    sh.block = sh.smem_tally ? (prec == 0 ? kSmtBlock64 : kSmtBlock32) : 256;
+    sh.block = sh.smem_tally ? (prec == 0 ? kSmtBlock64 : kSmtBlock32) : (prec == 0 ? kGlbBlock64 : kGlbBlock32);
     return sh;
 }
 
@@ -632,9 +632,9 @@ const void *transport_kernel_ptr(const CellArgs &ca, int prec) {
         if (prec == 1) return kptr<StF32, kSmtBlock32, true>(ca.geometry);
         return kptr<StF16, kSmtBlock32, true>(ca.geometry);
     }
-    if (prec == 0) return kptr<StF64, 256, false>(ca.geometry);
-    if (prec == 1) return kptr<StF32, 256, false>(ca.geometry);
-    return kptr<StF16, 256, false>(ca.geometry);
+    if (prec == 0) return kptr<StF64, kGlbBlock64, false>(ca.geometry);
+    if (prec == 1) return kptr<StF32, kGlbBlock32, false>(ca.geometry);
+    return kptr<StF16, kGlbBlock32, false>(ca.geometry);
 }
 
 template <class St, int B, bool SMT>
@@ -650,9 +650,9 @@ void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufPair buf, i
         else if (prec == 1) launch_one<StF32, kSmtBlock32, true>(ca, sc, buf, grid, sh.smem, st);
         else launch_one<StF16, kSmtBlock32, true>(ca, sc, buf, grid, sh.smem, st);
     } else {
-        if (prec == 0) launch_one<StF64, 256, false>(ca, sc, buf, grid, sh.smem, st);
-        else if (prec == 1) launch_one<StF32, 256, false>(ca, sc, buf, grid, sh.smem, st);
-        else launch_one<StF16, 256, false>(ca, sc, buf, grid, sh.smem, st);
+        if (prec == 0) launch_one<StF64, kGlbBlock64, false>(ca, sc, buf, grid, sh.smem, st);
+        else if (prec == 1) launch_one<StF32, kGlbBlock32, false>(ca, sc, buf, grid, sh.smem, st);
+        else launch_one<StF16, kGlbBlock32, false>(ca, sc, buf, grid, sh.smem, st);
     }
 }
 
@@ -666,8 +666,8 @@ template <class St, int B, bool SMT> static const void *wave_ptr(int which) {
 
 const void *surr_analog_ptr(const CellArgs &ca, int prec, int which) {
     const bool smt = transport_shape(ca, prec).smem_tally;
-    if (prec == 2) return smt ? wave_ptr<StF16, kSmtBlock32, true>(which) : wave_ptr<StF16, 256, false>(which);
-    return smt ? wave_ptr<StF32, kSmtBlock32, true>(which) : wave_ptr<StF32, 256, false>(which);
+    if (prec == 2) return smt ? wave_ptr<StF16, kSmtBlock32, true>(which) : wave_ptr<StF16, kGlbBlock32, false>(which);
+    return smt ? wave_ptr<StF32, kSmtBlock32, true>(which) : wave_ptr<StF32, kGlbBlock32, false>(which);
 }
 
 int surr_analog_smem(const CellArgs &ca, int prec) {
@@ -687,10 +687,10 @@ void launch_surr_analog(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs
     const bool smt = transport_shape(ca, prec).smem_tally;
     if (prec == 2) {
         if (smt) wave_one<StF16, kSmtBlock32, true>(ca, sc, bufs, w, which, round, grid, smem, st);
-        else wave_one<StF16, 256, false>(ca, sc, bufs, w, which, round, grid, smem, st);
+        else wave_one<StF16, kGlbBlock32, false>(ca, sc, bufs, w, which, round, grid, smem, st);
     } else {
         if (smt) wave_one<StF32, kSmtBlock32, true>(ca, sc, bufs, w, which, round, grid, smem, st);
-        else wave_one<StF32, 256, false>(ca, sc, bufs, w, which, round, grid, smem, st);
+        else wave_one<StF32, kGlbBlock32, false>(ca, sc, bufs, w, which, round, grid, smem, st);
     }
 }
 

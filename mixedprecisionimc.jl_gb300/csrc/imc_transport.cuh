@@ -39,9 +39,29 @@ template <bool SMT> __device__ __forceinline__ void add_limbs(long long *a, cons
         if (L.l1) atomicAdd_block(s + 1, (unsigned long long)L.l1);
         if (L.l2) atomicAdd_block(s + 2, (unsigned long long)L.l2);
     } else {
-        if (L.l0) atomicAdd((unsigned long long *)(a + 0), (unsigned long long)L.l0);
-        if (L.l1) atomicAdd((unsigned long long *)(a + 1), (unsigned long long)L.l1);
-        if (L.l2) atomicAdd((unsigned long long *)(a + 2), (unsigned long long)L.l2);
+        // Warp-aggregated: the lanes flushing to the same slot at this moment
+        // add their limbs in registers (integer sums, exact in any order) and
+        // one of them sends the reduction to L2.
+        const unsigned active = __activemask();
+        const unsigned peers = __match_any_sync(active, (unsigned long long)a);
+        const int lane = threadIdx.x & 31;
+        long long s0 = L.l0, s1 = L.l1, s2 = L.l2;
+        if (peers != (1u << lane)) {
+            const int rank = __popc(peers & ((1u << lane) - 1u));
+            const int n = __popc(peers);
+            for (int off = 1; off < n; off <<= 1) {
+                const int pr = rank + off;
+                const int src = pr < n ? (int)__fns(peers, 0u, pr + 1) : lane;
+                const long long o0 = __shfl_sync(peers, s0, src);
+                const long long o1 = __shfl_sync(peers, s1, src);
+                const long long o2 = __shfl_sync(peers, s2, src);
+                if ((rank & (2 * off - 1)) == 0 && pr < n) { s0 += o0; s1 += o1; s2 += o2; }
+            }
+            if (rank != 0) return;
+        }
+        if (s0) atomicAdd((unsigned long long *)(a + 0), (unsigned long long)s0);
+        if (s1) atomicAdd((unsigned long long *)(a + 1), (unsigned long long)s1);
+        if (s2) atomicAdd((unsigned long long *)(a + 2), (unsigned long long)s2);
     }
 }
 
@@ -98,6 +118,11 @@ __device__ __forceinline__ void flush_one(long long *acc, int slot, T v, int b, 
 // most of the shared memory)
 constexpr int kSmtBlock32 = 1024;
 constexpr int kSmtBlock64 = 512;
+// threads per block of the global-tally kernels (meshes whose private
+// tallies do not fit): FP32 / FP16 state as one 1024-thread block per SM,
+// FP64 in 256-thread blocks
+constexpr int kGlbBlock32 = 1024;
+constexpr int kGlbBlock64 = 256;
 
 // 1D per-cell table: sigma_a f, effective scatter, width * distancescale,
 // width; the FP32 table adds the reciprocals its arithmetic multiplies by
