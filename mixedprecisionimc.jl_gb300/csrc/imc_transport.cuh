@@ -31,13 +31,32 @@ template <class T> __device__ __forceinline__ void nadd(T &s, T &c, T x) {
 
 // Limb adds into global memory (64-bit integer reductions in L2) or into the
 // block's private copy of the tally in shared memory.
+//
+// A shared-memory slot is six 32-bit words: the running sums of the three
+// limb positions (w[0..2], same order as Limbs l0..l2, wrapping modulo 2^32)
+// and their signed carry counts (cy[0..2]).  Each limb is added with a native
+// 32-bit shared atomic; the returned old sum shows whether the add wrapped,
+// and only then the carry count is bumped (a negative limb l is added as
+// 2^32 + l with a carry of -1).  flush_block_tallies folds the carries into
+// the next limb up.  Exact for any order of adds, like the 64-bit form, at
+// the cost of a 32-bit atomic instead of a 64-bit one (which shared memory
+// does not add natively).  The carry counts stay below 2^31 in magnitude
+// while a block adds fewer than 2^31 limbs to one slot in one launch.
+__device__ __forceinline__ void add_word_smem(unsigned *w, int *cy, long long l) {
+    const unsigned u = (unsigned)l;
+    const unsigned old = atomicAdd_block(w, u);
+    const int c = (old + u < old ? 1 : 0) - (l < 0 ? 1 : 0);
+    if (c) atomicAdd_block(cy, c);
+}
+
 template <bool SMT> __device__ __forceinline__ void add_limbs(long long *a, const Limbs &L) {
     if (SMT) {
         // the pointer is known to address shared memory
-        unsigned long long *s = (unsigned long long *)a;
-        if (L.l0) atomicAdd_block(s + 0, (unsigned long long)L.l0);
-        if (L.l1) atomicAdd_block(s + 1, (unsigned long long)L.l1);
-        if (L.l2) atomicAdd_block(s + 2, (unsigned long long)L.l2);
+        unsigned *w = reinterpret_cast<unsigned *>(a);
+        int *cy = reinterpret_cast<int *>(a) + 3;
+        if (L.l0) add_word_smem(w + 0, cy + 0, L.l0);
+        if (L.l1) add_word_smem(w + 1, cy + 1, L.l1);
+        if (L.l2) add_word_smem(w + 2, cy + 2, L.l2);
     } else {
         // Warp-aggregated: the lanes flushing to the same slot at this moment
         // add their limbs in registers (integer sums, exact in any order) and
@@ -78,14 +97,21 @@ __device__ __forceinline__ long long *tally_smem(unsigned char *smem, int table)
 }
 
 // Adds the block's shared tallies (deposition, then census energy, in the
-// same 3-limb layout as the global accumulators) to the global ones.
+// same 3-limb layout as the global accumulators) to the global ones: limb
+// q of a slot gets its word sum plus the carries out of the limb below it.
 __device__ __forceinline__ void flush_block_tallies(const CellArgs &ca, const long long *sm) {
     __syncthreads();
-    const int n = 3 * ca.K * ca.nc;
+    const int n = ca.K * ca.nc;
     for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) {
-        long long v = sm[i];
-        if (v) atomicAdd((unsigned long long *)((i < n ? ca.dep_acc : ca.rad_acc) + (i < n ? i : i - n)),
-                         (unsigned long long)v);
+        const unsigned *w = reinterpret_cast<const unsigned *>(sm + 3 * (size_t)i);
+        const int *cy = reinterpret_cast<const int *>(w + 3);
+        long long *g = (i < n ? ca.dep_acc : ca.rad_acc) + 3 * (size_t)(i < n ? i : i - n);
+        const long long v0 = (long long)w[0] + (long long)cy[1] + (long long)cy[0] * 4294967296ll;
+        const long long v1 = (long long)w[1] + (long long)cy[2];
+        const long long v2 = (long long)w[2];
+        if (v0) atomicAdd((unsigned long long *)(g + 0), (unsigned long long)v0);
+        if (v1) atomicAdd((unsigned long long *)(g + 1), (unsigned long long)v1);
+        if (v2) atomicAdd((unsigned long long *)(g + 2), (unsigned long long)v2);
     }
 }
 
