@@ -121,24 +121,64 @@ IMC_HD bool sel_finite_half(float v) {
     return v == v && fabsf(v) < 65520.0f;
 }
 
+// Julia's isless order on Float64 as an unsigned integer key: -Inf < ... <
+// -0.0 < +0.0 < ... < +Inf < NaN, every NaN equal (the sign-magnitude bits
+// flipped into a two's-complement-free order).  Sorting by the key is sorting
+// with jisless, with integer compares instead of FP64 ones (1/64 rate).
+IMC_HD uint64_t isless_key(double v) {
+    uint64_t b;
+#ifdef __CUDA_ARCH__
+    b = (uint64_t)__double_as_longlong(v);
+#else
+    memcpy(&b, &v, 8);
+#endif
+    if (v != v) return ~0ull;
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+IMC_HD double isless_value(uint64_t k) {
+    uint64_t b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;  // NaN key -> a NaN
+    double v;
+#ifdef __CUDA_ARCH__
+    v = __longlong_as_double((long long)b);
+#else
+    memcpy(&v, &b, 8);
+#endif
+    return v;
+}
+
 // Utilities.sorter (src/imc_utilities.jl:23-54): append scale j, sort
 // ascending, multiply smallest by largest pairwise; the first scale whose
 // product is finite in the selection precision wins.  Returns the FP64
-// product; *jout = -1 if no scale works.  n <= 15.
-template <int SEL>
-IMC_HD double sorter(const double *vals, int n, const double *scales, int nsc, int *jout) {
-    double arr[16];
+// product; *jout = -1 if no scale works.  N values (compile time).
+//
+// The sort is a stable adjacent-swap insertion sort, unrolled over the
+// compile-time size so the keys stay in registers.  Values that compare
+// equal under isless have equal bits, except NaNs, whose products are never
+// finite, so the product is the reference's in every case.
+template <int SEL, int N>
+IMC_HD double sorter_n(const double *vals, const double *scales, int nsc, int *jout) {
+    constexpr int m = N + 1;
+    uint64_t base[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) base[i] = isless_key(vals[i]);
     for (int j = 0; j < nsc; ++j) {
-        int m = n + 1;
-        for (int i = 0; i < n; ++i) arr[i] = vals[i];
-        arr[n] = scales[j];
-        // insertion sort (stable) with isless ordering
+        uint64_t k[m];
+#pragma unroll
+        for (int i = 0; i < N; ++i) k[i] = base[i];
+        k[N] = isless_key(scales[j]);
+#pragma unroll
         for (int i = 1; i < m; ++i) {
-            double key = arr[i];
-            int q = i - 1;
-            while (q >= 0 && jisless(key, arr[q])) { arr[q + 1] = arr[q]; --q; }
-            arr[q + 1] = key;
+#pragma unroll
+            for (int q = i - 1; q >= 0; --q) {
+                const uint64_t a = k[q], b = k[q + 1];
+                const bool sw = b < a;
+                k[q] = sw ? b : a;
+                k[q + 1] = sw ? a : b;
+            }
         }
+        double arr[m];
+#pragma unroll
+        for (int i = 0; i < m; ++i) arr[i] = isless_value(k[i]);
         double prod = 1.0;
         bool ok;
         if (SEL == 2) {
@@ -146,6 +186,7 @@ IMC_HD double sorter(const double *vals, int n, const double *scales, int nsc, i
             // in binary32, so one rounding to binary16 per step reproduces
             // native half arithmetic.
             float ph = 1.0f;
+#pragma unroll
             for (int i = 0; i < m / 2; ++i) {
                 prod *= arr[i] * arr[m - 1 - i];
                 float a = __half2float(__double2half(arr[i])), b = __half2float(__double2half(arr[m - 1 - i]));
@@ -160,6 +201,7 @@ IMC_HD double sorter(const double *vals, int n, const double *scales, int nsc, i
             ok = sel_finite_half(ph);
         } else if (SEL == 1) {
             float pf = 1.0f;
+#pragma unroll
             for (int i = 0; i < m / 2; ++i) {
                 prod *= arr[i] * arr[m - 1 - i];
                 pf = pf * ((float)arr[i] * (float)arr[m - 1 - i]);
@@ -170,6 +212,7 @@ IMC_HD double sorter(const double *vals, int n, const double *scales, int nsc, i
             }
             ok = isfinite(pf);
         } else {
+#pragma unroll
             for (int i = 0; i < m / 2; ++i) prod *= arr[i] * arr[m - 1 - i];
             if (m & 1) prod *= arr[m / 2];
             ok = true;
@@ -181,6 +224,29 @@ IMC_HD double sorter(const double *vals, int n, const double *scales, int nsc, i
     }
     *jout = -1;
     return 0.0;
+}
+
+// the same with the number of values at run time (host checks); n <= 15
+template <int SEL>
+IMC_HD double sorter(const double *vals, int n, const double *scales, int nsc, int *jout) {
+    switch (n) {
+    case 1: return sorter_n<SEL, 1>(vals, scales, nsc, jout);
+    case 2: return sorter_n<SEL, 2>(vals, scales, nsc, jout);
+    case 3: return sorter_n<SEL, 3>(vals, scales, nsc, jout);
+    case 4: return sorter_n<SEL, 4>(vals, scales, nsc, jout);
+    case 5: return sorter_n<SEL, 5>(vals, scales, nsc, jout);
+    case 6: return sorter_n<SEL, 6>(vals, scales, nsc, jout);
+    case 7: return sorter_n<SEL, 7>(vals, scales, nsc, jout);
+    case 8: return sorter_n<SEL, 8>(vals, scales, nsc, jout);
+    case 9: return sorter_n<SEL, 9>(vals, scales, nsc, jout);
+    case 10: return sorter_n<SEL, 10>(vals, scales, nsc, jout);
+    case 11: return sorter_n<SEL, 11>(vals, scales, nsc, jout);
+    case 12: return sorter_n<SEL, 12>(vals, scales, nsc, jout);
+    case 13: return sorter_n<SEL, 13>(vals, scales, nsc, jout);
+    case 14: return sorter_n<SEL, 14>(vals, scales, nsc, jout);
+    case 15: return sorter_n<SEL, 15>(vals, scales, nsc, jout);
+    default: *jout = -1; return 0.0;
+    }
 }
 
 // ------------------------------------------------- fixed-point tallies

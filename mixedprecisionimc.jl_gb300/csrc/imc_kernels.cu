@@ -70,13 +70,15 @@ __global__ void __launch_bounds__(kCellThreads) k_update(CellArgs ca, Scalars *s
     }
     ca.beta[i] = beta;
     double Tc = (ca.temp_floor > 0.0 && T < ca.temp_floor) ? ca.temp_floor : T;
-    double sa = ca.sa_val[i] * pow(Tc, ca.sa_pow[i]);
+    // pow(x, 0) is 1 for every x (NaN included): skip the FP64 pow there
+    const double psa = ca.sa_pow[i], pss = ca.ss_pow[i];
+    double sa = ca.sa_val[i] * (psa == 0.0 ? 1.0 : pow(Tc, psa));
     if (ca.marshak) sa = ca.sa_val[i] / Tc / Tc / Tc;
     ca.sa[i] = sa;
-    ca.ss[i] = ca.ss_val[i] * pow(Tc, ca.ss_pow[i]);
+    ca.ss[i] = ca.ss_val[i] * (pss == 0.0 ? 1.0 : pow(Tc, pss));
     double v[6] = {ca.ds, ca.alpha, beta, c, dt, sa};
     int j;
-    double prod = sorter<0>(v, 6, one, 1, &j);
+    double prod = sorter_n<0, 6>(v, one, 1, &j);
     ca.fleck[i] = 1.0 / (1.0 + prod);
 }
 
@@ -85,10 +87,11 @@ void launch_update(const CellArgs &ca, Scalars *sc, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------- sourcing
-__device__ __forceinline__ double sorter_sel(int sel, const double *v, int n, const double *sc, int K, int *j) {
-    if (sel == 2) return sorter<2>(v, n, sc, K, j);
-    if (sel == 1) return sorter<1>(v, n, sc, K, j);
-    return sorter<0>(v, n, sc, K, j);
+template <int N>
+__device__ __forceinline__ double sorter_sel(int sel, const double *v, const double *sc, int K, int *j) {
+    if (sel == 2) return sorter_n<2, N>(v, sc, K, j);
+    if (sel == 1) return sorter_n<1, N>(v, sc, K, j);
+    return sorter_n<0, N>(v, sc, K, j);
 }
 
 __device__ __forceinline__ int nsurf_slots(const CellArgs &ca) {
@@ -126,12 +129,12 @@ __global__ void __launch_bounds__(kCellThreads) k_source_slots(CellArgs ca, Scal
             double Ts = ca.tsurf[s], w = 0.0;
             if (ca.geometry == 1) {
                 double v[8] = {a, c, Ts, Ts, Ts, Ts, dt, 0.25};
-                e = sorter_sel(ca.sel_prec, v, 8, ca.scales, K, &j);
+                e = sorter_sel<8>(ca.sel_prec, v, ca.scales, K, &j);
             } else {
                 if (s < 2 * ca.nx) w = ca.dx[s % ca.nx];
                 else w = ca.dy[(s - 2 * ca.nx) % ca.ny];
                 double v[9] = {a, c, Ts, Ts, Ts, Ts, w, dt, 0.25};
-                e = sorter_sel(ca.sel_prec, v, 9, ca.scales, K, &j);
+                e = sorter_sel<9>(ca.sel_prec, v, ca.scales, K, &j);
             }
         } else if (s < ns + nc) {
             const int i = s - ns;
@@ -140,15 +143,15 @@ __global__ void __launch_bounds__(kCellThreads) k_source_slots(CellArgs ca, Scal
             const double T = ca.temp[i], f = ca.fleck[i], sa = ca.sa[i];
             if (ca.geometry == 1) {
                 double v[11] = {f, sa, a, c, T, T, T, T, ca.dx[i], dt, ds};
-                e = sorter_sel(ca.sel_prec, v, 11, ca.scales, K, &j);
+                e = sorter_sel<11>(ca.sel_prec, v, ca.scales, K, &j);
             } else {
                 double v[12] = {f, sa, a, c, T, T, T, T, ca.dx[ix], ca.dy[iy], dt, ds};
-                e = sorter_sel(ca.sel_prec, v, 12, ca.scales, K, &j);
+                e = sorter_sel<12>(ca.sel_prec, v, ca.scales, K, &j);
             }
             // emitted energy density (src/imc_sourcing.jl:69-70)
             double ve[10] = {f, sa, a, c, T, T, T, T, dt, ds};
             int je;
-            double em = sorter_sel(ca.sel_prec, ve, 10, ca.scales, K, &je);
+            double em = sorter_sel<10>(ca.sel_prec, ve, ca.scales, K, &je);
             for (int k = 0; k < K; ++k) ca.emitted[(size_t)k * nc + i] = 0.0;
             if (je >= 0) ca.emitted[(size_t)je * nc + i] = em;
             else atomicOr(&sc->flags, 1u << 5);
@@ -158,10 +161,10 @@ __global__ void __launch_bounds__(kCellThreads) k_source_slots(CellArgs ca, Scal
             const int iy = ca.geometry == 1 ? 0 : i / ca.nx;
             if (ca.geometry == 1) {
                 double v[3] = {ca.radsource[i], ca.dx[i], dt};
-                e = sorter_sel(ca.sel_prec, v, 3, ca.scales, K, &j);
+                e = sorter_sel<3>(ca.sel_prec, v, ca.scales, K, &j);
             } else {
                 double v[4] = {ca.radsource[i], ca.dx[ix], ca.dy[iy], dt};
-                e = sorter_sel(ca.sel_prec, v, 4, ca.scales, K, &j);
+                e = sorter_sel<4>(ca.sel_prec, v, ca.scales, K, &j);
             }
         }
         if (j < 0) atomicOr(&sc->flags, 1u << 5);
@@ -767,7 +770,7 @@ __global__ void __launch_bounds__(kCellThreads) k_tally(CellArgs ca, Scalars *sc
             double T = ca.temp[i];
             double v[10] = {ca.fleck[i], ca.sa[i], a, c, T, T, T, T, dt, ca.ds};
             int j;
-            ca.matenergydens[i] = sorter<0>(v, 10, one, 1, &j);
+            ca.matenergydens[i] = sorter_n<0, 10>(v, one, 1, &j);
         }
         double inc = 0.0;
         for (int k = 0; k < K; ++k)

@@ -48,11 +48,13 @@ int main() {
         } else if (cmd == "R") {
             int prec, n, K;
             in >> prec >> n;
+            // values as strtod tokens, so nan, inf and -0.0 pass through
+            std::string t;
             std::vector<double> v(n);
-            for (auto &x : v) in >> x;
+            for (auto &x : v) { in >> t; x = strtod(t.c_str(), nullptr); }
             in >> K;
             std::vector<double> s(K);
-            for (auto &x : s) in >> x;
+            for (auto &x : s) { in >> t; x = strtod(t.c_str(), nullptr); }
             int j;
             double p = prec == 0 ? sorter<0>(v.data(), n, s.data(), K, &j)
                      : prec == 1 ? sorter<1>(v.data(), n, s.data(), K, &j)

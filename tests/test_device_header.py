@@ -94,3 +94,28 @@ def test_sorter_matches_oracle(tool, prec):
         p, _, jo = oracle.sorter(v, s, prec)
         assert int(j) == jo
         assert float.fromhex(p_hex) == p
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_sorter_special_values_match_oracle(tool, prec):
+    """isless order with signed zeros, infinities, NaN, negatives and ties:
+    the register sort of the device header (integer isless keys) picks the
+    same product and scale as the oracle's restated insertion sort."""
+    rng = np.random.default_rng(10 + prec)
+    special = [0.0, -0.0, np.inf, -np.inf, np.nan, -1.5, 2.0, 2.0, 1e-300, -1e300, 3.0e38, 7e4]
+    lines, cases = [], []
+    for _ in range(200):
+        n = int(rng.integers(1, 13))
+        v = [float(special[k]) if rng.uniform() < 0.5 else float(10.0 ** rng.uniform(-8, 8))
+             for k in rng.integers(0, len(special), n)]
+        s = [float(x) for x in rng.choice([1.0, 2.0 ** -30, 2.0 ** 30, -4.0, 0.0], int(rng.integers(1, 4)))]
+        lines.append("R %d %d %s %d %s" % (prec, n, " ".join(repr(x) for x in v), len(s),
+                                           " ".join(repr(x) for x in s)))
+        cases.append((v, s))
+    out = tool(lines)
+    for (v, s), o in zip(cases, out):
+        p_hex, j = o.split()
+        p, _, jo = oracle.sorter(v, s, prec)
+        assert int(j) == jo, (v, s)
+        pg = float.fromhex(p_hex)
+        assert pg == p and np.signbit(pg) == np.signbit(p), (v, s, pg, p)
