@@ -342,11 +342,11 @@ int enqueue_step(ImcHandle *h, bool with_events, int ev_slot) {
     if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot], st));
     run_transport(h, bufs, st);
     if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot + 1], st));
-    launch_finalize(h->ca, h->d_sc, st);
+    // finalize + tally, then the compaction (it touches no cell field), then
+    // energycheck + timestep: the reference's order in four launches
+    launch_finalize_tally(h->ca, h->d_sc, st);
     launch_compact(h->ca, h->d_sc, h->prec, bufs, h->tile_cnt, h->tile_off, h->ntiles_cap, false, st);
-    launch_tally(h->ca, h->d_sc, st);
-    launch_energycheck(h->ca, h->d_sc, h->d_stats, h->stats_cap, st);
-    launch_timestep(h->ca, h->d_sc, st);
+    launch_energycheck_timestep(h->ca, h->d_sc, h->d_stats, h->stats_cap, st);
     CKL(h);
     return IMC_OK;
 }
@@ -1256,9 +1256,10 @@ int imc_get_surrogate_active(const ImcHandle *h, int *active) {
 
 int imc_kernels_per_step(const ImcHandle *h, int *count) {
     if (!h || !count) return IMC_ERR_INVALID_ARG;
-    // update, source x5, transport, finalize, compact x4, tally, energycheck,
-    // timestep; the surrogate transport is 1 + 2 kSurrRounds kernels
-    *count = 15 + (h->ca.surr_image ? 2 * kSurrRounds : 0);
+    // update, source x5, transport, finalize + tally, compact x4,
+    // energycheck + timestep; the surrogate transport is 1 + 2 kSurrRounds
+    // kernels
+    *count = 13 + (h->ca.surr_image ? 2 * kSurrRounds : 0);
     return IMC_OK;
 }
 

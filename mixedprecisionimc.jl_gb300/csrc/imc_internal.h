@@ -159,6 +159,10 @@ void launch_finalize(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 void launch_tally(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 void launch_energycheck(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap, cudaStream_t st);
 void launch_timestep(const CellArgs &ca, Scalars *sc, cudaStream_t st);
+// the step sequence's fused launches: finalize + tally, energycheck + timestep
+void launch_finalize_tally(const CellArgs &ca, Scalars *sc, cudaStream_t st);
+void launch_energycheck_timestep(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap,
+                                 cudaStream_t st);
 void launch_prepare_transport(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 const void *transport_kernel_ptr(const CellArgs &ca, int prec);
 

@@ -87,12 +87,6 @@ void launch_update(const CellArgs &ca, Scalars *sc, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------- sourcing
-template <int N>
-__device__ __forceinline__ double sorter_sel(int sel, const double *v, const double *sc, int K, int *j) {
-    if (sel == 2) return sorter_n<2, N>(v, sc, K, j);
-    if (sel == 1) return sorter_n<1, N>(v, sc, K, j);
-    return sorter_n<0, N>(v, sc, K, j);
-}
 
 __device__ __forceinline__ int nsurf_slots(const CellArgs &ca) {
     return ca.geometry == 1 ? 2 : 2 * ca.nx + 2 * ca.ny;
@@ -115,6 +109,7 @@ __device__ __forceinline__ int slot_group(const CellArgs &ca, int s) {
 // reference's push! order: 1D [left, right, body cells, source cells]; 2D
 // [bottom x, top x, left y, right y, body cells, source cells].  Each block
 // also leaves double-double partial sums of e/escale per slot group.
+template <int G, int SEL>
 __global__ void __launch_bounds__(kCellThreads) k_source_slots(CellArgs ca, Scalars *sc) {
     __shared__ DD sh[kCellThreads];
     const double a = ca.a, c = ca.c, ds = ca.ds, dt = sc->dt;
@@ -127,44 +122,44 @@ __global__ void __launch_bounds__(kCellThreads) k_source_slots(CellArgs ca, Scal
         int j = -1;
         if (s < ns) {
             double Ts = ca.tsurf[s], w = 0.0;
-            if (ca.geometry == 1) {
+            if (G == 1) {
                 double v[8] = {a, c, Ts, Ts, Ts, Ts, dt, 0.25};
-                e = sorter_sel<8>(ca.sel_prec, v, ca.scales, K, &j);
+                e = sorter_n<SEL, 8>(v, ca.scales, K, &j);
             } else {
                 if (s < 2 * ca.nx) w = ca.dx[s % ca.nx];
                 else w = ca.dy[(s - 2 * ca.nx) % ca.ny];
                 double v[9] = {a, c, Ts, Ts, Ts, Ts, w, dt, 0.25};
-                e = sorter_sel<9>(ca.sel_prec, v, ca.scales, K, &j);
+                e = sorter_n<SEL, 9>(v, ca.scales, K, &j);
             }
         } else if (s < ns + nc) {
             const int i = s - ns;
-            const int ix = ca.geometry == 1 ? i : i % ca.nx;
-            const int iy = ca.geometry == 1 ? 0 : i / ca.nx;
+            const int ix = G == 1 ? i : i % ca.nx;
+            const int iy = G == 1 ? 0 : i / ca.nx;
             const double T = ca.temp[i], f = ca.fleck[i], sa = ca.sa[i];
-            if (ca.geometry == 1) {
+            if (G == 1) {
                 double v[11] = {f, sa, a, c, T, T, T, T, ca.dx[i], dt, ds};
-                e = sorter_sel<11>(ca.sel_prec, v, ca.scales, K, &j);
+                e = sorter_n<SEL, 11>(v, ca.scales, K, &j);
             } else {
                 double v[12] = {f, sa, a, c, T, T, T, T, ca.dx[ix], ca.dy[iy], dt, ds};
-                e = sorter_sel<12>(ca.sel_prec, v, ca.scales, K, &j);
+                e = sorter_n<SEL, 12>(v, ca.scales, K, &j);
             }
             // emitted energy density (src/imc_sourcing.jl:69-70)
             double ve[10] = {f, sa, a, c, T, T, T, T, dt, ds};
             int je;
-            double em = sorter_sel<10>(ca.sel_prec, ve, ca.scales, K, &je);
+            double em = sorter_n<SEL, 10>(ve, ca.scales, K, &je);
             for (int k = 0; k < K; ++k) ca.emitted[(size_t)k * nc + i] = 0.0;
             if (je >= 0) ca.emitted[(size_t)je * nc + i] = em;
             else atomicOr(&sc->flags, 1u << 5);
         } else {
             const int i = s - ns - nc;
-            const int ix = ca.geometry == 1 ? i : i % ca.nx;
-            const int iy = ca.geometry == 1 ? 0 : i / ca.nx;
-            if (ca.geometry == 1) {
+            const int ix = G == 1 ? i : i % ca.nx;
+            const int iy = G == 1 ? 0 : i / ca.nx;
+            if (G == 1) {
                 double v[3] = {ca.radsource[i], ca.dx[i], dt};
-                e = sorter_sel<3>(ca.sel_prec, v, ca.scales, K, &j);
+                e = sorter_n<SEL, 3>(v, ca.scales, K, &j);
             } else {
                 double v[4] = {ca.radsource[i], ca.dx[ix], ca.dy[iy], dt};
-                e = sorter_sel<4>(ca.sel_prec, v, ca.scales, K, &j);
+                e = sorter_n<SEL, 4>(v, ca.scales, K, &j);
             }
         }
         if (j < 0) atomicOr(&sc->flags, 1u << 5);
@@ -502,7 +497,11 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
 
 void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufPair buf, int grid, cudaStream_t st) {
     const int nb = ca.nblk_slot;
-    k_source_slots<<<nb, kCellThreads, 0, st>>>(ca, sc);
+    // one instantiation per geometry and scale-selection precision, so each
+    // holds only its own unrolled sorters
+    auto slots = ca.geometry == 1 ? (ca.sel_prec == 2 ? k_source_slots<1, 2> : ca.sel_prec == 1 ? k_source_slots<1, 1> : k_source_slots<1, 0>)
+                                  : (ca.sel_prec == 2 ? k_source_slots<2, 2> : ca.sel_prec == 1 ? k_source_slots<2, 1> : k_source_slots<2, 0>);
+    slots<<<nb, kCellThreads, 0, st>>>(ca, sc);
     k_source_total<<<1, 192, 0, st>>>(ca, sc);
     k_source_counts<<<nb, kCellThreads, 0, st>>>(ca, sc);
     k_source_scan<<<1, kPlanThreads, 0, st>>>(ca, sc);
@@ -715,11 +714,11 @@ __device__ __forceinline__ double cell_vol(const CellArgs &ca, int i) {
 // Converts this transport's fixed-point tallies to FP64 mesh fields and
 // clears the accumulators: energydep and the escaped energy as
 // Transport.MC leaves them (src/imc_transport.jl:198-205), and the census
-// radiation energy density of src/imc_tally.jl:81-113.
-__global__ void __launch_bounds__(kCellThreads) k_finalize(CellArgs ca, Scalars *sc) {
+// radiation energy density of src/imc_tally.jl:81-113.  Cell i, and the
+// escaped energy and segment statistics in block 0, thread 0.
+__device__ __forceinline__ void finalize_cell(const CellArgs &ca, Scalars *sc, int i) {
     const int nc = ca.nc, K = ca.K;
     const int b_dep = sc->b_dep, b_rad = sc->b_rad, b_lost = sc->b_lost;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nc) {
         const double vol = cell_vol(ca, i);
         double r = 0.0;
@@ -750,19 +749,13 @@ __global__ void __launch_bounds__(kCellThreads) k_finalize(CellArgs ca, Scalars 
     }
 }
 
-void launch_finalize(const CellArgs &ca, Scalars *sc, cudaStream_t st) {
-    k_finalize<<<ca.nblk_cell, kCellThreads, 0, st>>>(ca, sc);
-}
-
 // Tally.tally per cell (src/imc_tally.jl:29-75); each block leaves partial
 // sums of the deposited energy per scale and of the radiation energy.
-__global__ void __launch_bounds__(kCellThreads) k_tally(CellArgs ca, Scalars *sc) {
-    __shared__ DD sh[kCellThreads];
+__device__ __forceinline__ void tally_cell(const CellArgs &ca, Scalars *sc, int i, DD *sh) {
     const int nc = ca.nc, K = ca.K;
     const double a = ca.a, c = ca.c, dt = sc->dt;
     const bool first = sc->t == 0.0;
     const double one[1] = {1.0};
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double vol = 0.0;
     if (i < nc) {
         vol = cell_vol(ca, i);
@@ -796,12 +789,64 @@ __global__ void __launch_bounds__(kCellThreads) k_tally(CellArgs ca, Scalars *sc
     }
 }
 
+__global__ void __launch_bounds__(kCellThreads) k_finalize(CellArgs ca, Scalars *sc) {
+    finalize_cell(ca, sc, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(kCellThreads) k_tally(CellArgs ca, Scalars *sc) {
+    __shared__ DD sh[kCellThreads];
+    tally_cell(ca, sc, blockIdx.x * blockDim.x + threadIdx.x, sh);
+}
+
+// Both in one launch (the step sequence): the tally of cell i reads only
+// what the finalize of cell i wrote, in the same thread, and nothing that
+// the compaction between them in the reference's order changes.
+__global__ void __launch_bounds__(kCellThreads) k_finalize_tally(CellArgs ca, Scalars *sc) {
+    __shared__ DD sh[kCellThreads];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    finalize_cell(ca, sc, i);
+    tally_cell(ca, sc, i, sh);
+}
+
+void launch_finalize(const CellArgs &ca, Scalars *sc, cudaStream_t st) {
+    k_finalize<<<ca.nblk_cell, kCellThreads, 0, st>>>(ca, sc);
+}
+
 void launch_tally(const CellArgs &ca, Scalars *sc, cudaStream_t st) {
     k_tally<<<ca.nblk_cell, kCellThreads, 0, st>>>(ca, sc);
 }
 
+void launch_finalize_tally(const CellArgs &ca, Scalars *sc, cudaStream_t st) {
+    k_finalize_tally<<<ca.nblk_cell, kCellThreads, 0, st>>>(ca, sc);
+}
+
+// timestep (src/MixedPrecisionIMC.jl:181-222), FP64 on the device so a run
+// can replay without host round trips.
+__device__ __forceinline__ void advance_clock(const CellArgs &ca, Scalars *sc) {
+    double t = sc->t, dt = sc->dt;
+    const double t_end = ca.t_end;
+    if (t == t_end) {
+        t = t_end + dt;
+    } else if (ca.timestepping == 0) {
+        if (t + dt > t_end) { dt = t_end - t; t = t_end; }
+        else t = t + dt;
+    } else {
+        if (dt < ca.dtmax) {
+            dt = dt * ca.kfac;
+            if (dt > ca.dtmax) dt = ca.dtmax;
+        }
+        if (t + dt > t_end) { dt = t_end - t; t = t_end; }
+        else t = t + dt;
+    }
+    sc->t = t;
+    sc->dt = dt;
+    sc->finished = t > t_end ? 1 : 0;
+    sc->step += 1u;
+}
+
 // EnergyCheck.energychecker (src/imc_energycheck.jl:19-38).  One warp per
 // partial-sum group (K deposition scales, then the radiation energy).
+template <bool STEP>
 __global__ void __launch_bounds__(544) k_energycheck(CellArgs ca, Scalars *sc, DevStats *stats, long long stats_cap) {
     __shared__ double g[17];
     const int warp = threadIdx.x >> 5, np = ca.K + 1;
@@ -837,37 +882,21 @@ __global__ void __launch_bounds__(544) k_energycheck(CellArgs ca, Scalars *sc, D
     sc->radenergy = radenergy;
     sc->radenergyold = radenergy;
     sc->lostenergy = 0.0;
+    if (STEP) advance_clock(ca, sc);  // the step sequence: timestep in the same launch
 }
 
-void launch_energycheck(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap, cudaStream_t st) {
-    k_energycheck<<<1, 32 * (ca.K + 1), 0, st>>>(ca, sc, stats, stats_cap);
-}
-
-// timestep (src/MixedPrecisionIMC.jl:181-222), FP64 on the device so a run
-// can replay without host round trips.
-__global__ void k_timestep(CellArgs ca, Scalars *sc) {
-    double t = sc->t, dt = sc->dt;
-    const double t_end = ca.t_end;
-    if (t == t_end) {
-        t = t_end + dt;
-    } else if (ca.timestepping == 0) {
-        if (t + dt > t_end) { dt = t_end - t; t = t_end; }
-        else t = t + dt;
-    } else {
-        if (dt < ca.dtmax) {
-            dt = dt * ca.kfac;
-            if (dt > ca.dtmax) dt = ca.dtmax;
-        }
-        if (t + dt > t_end) { dt = t_end - t; t = t_end; }
-        else t = t + dt;
-    }
-    sc->t = t;
-    sc->dt = dt;
-    sc->finished = t > t_end ? 1 : 0;
-    sc->step += 1u;
-}
+__global__ void k_timestep(CellArgs ca, Scalars *sc) { advance_clock(ca, sc); }
 
 void launch_timestep(const CellArgs &ca, Scalars *sc, cudaStream_t st) { k_timestep<<<1, 1, 0, st>>>(ca, sc); }
+
+void launch_energycheck(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap, cudaStream_t st) {
+    k_energycheck<false><<<1, 32 * (ca.K + 1), 0, st>>>(ca, sc, stats, stats_cap);
+}
+
+void launch_energycheck_timestep(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap,
+                                 cudaStream_t st) {
+    k_energycheck<true><<<1, 32 * (ca.K + 1), 0, st>>>(ca, sc, stats, stats_cap);
+}
 
 // Transport of a list that was set directly (no sourcing this step): take the
 // fixed-point exponents from the census maximum.
