@@ -308,7 +308,7 @@ def c5_section(n_err=16):
             if params is not None:
                 for e in engines:
                     e.set_surrogate(params)
-            steps, wall = mpimc.run_batch(engines, threads=16)
+            steps, wall = mpimc.run_batch(engines, threads=32)
             tot = np.array([e.totals() for e in engines], dtype=np.float64)
             temps = [e.field("temp") for e in engines]
         finally:

@@ -59,7 +59,13 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     float *gate = reinterpret_cast<float *>(smem_raw + analog1d_smem(ca, sizeof(T), SMT, false));
     for (int i = threadIdx.x; i < N; i += blockDim.x) tab[i] = make_tab1<T>(ca.sa[i], ca.fleck[i], ca.ss[i], ca.dx[i], ds);
     if (kPause) fill_gate<T>(ca, gate, ds, c, endsteptime);
-    __syncthreads();
+    // the barrier after the table; with the gate, also whether any cell's
+    // gate is open this step (each thread tests the entries it filled; every
+    // block fills the whole gate, so all blocks agree): if none is, no
+    // history is tested
+    bool gating = false;
+    if (kPause) gating = __syncthreads_or(gate_open(ca, gate));
+    else __syncthreads();
     const int b_dep = sc->b_dep, b_rad = sc->b_rad, b_lost = sc->b_lost;
     const unsigned step = sc->step;
     const unsigned long long seed = ca.seed;
@@ -117,7 +123,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     // one pass of the reference's while loop; 0 = go on, 1 = killed or
     // escaped, 2 = census, 3 = set aside for a query (kPause)
     auto segment = [&]() -> int {
-        if (kPause && (float)(x < tab[cell].dxs - x ? x : tab[cell].dxs - x) * (float)tab[cell].seff >= gate[cell]) {
+        if (gating && (float)(x < tab[cell].dxs - x ? x : tab[cell].dxs - x) * (float)tab[cell].seff >= gate[cell]) {
             Query q;
             const int kind = surr_decide<T>(tab[cell], x, mu, t, E, minenergy, c, ds, endsteptime, q);
             if (kind == kCertainKill) {

@@ -292,6 +292,13 @@ __device__ __forceinline__ void fill_gate(const CellArgs &ca, float *gate, T ds,
     }
 }
 
+// whether this thread's share of the filled gate holds an open cell
+__device__ __forceinline__ bool gate_open(const CellArgs &ca, const float *gate) {
+    bool open = false;
+    for (int i = threadIdx.x; i < ca.nx; i += blockDim.x) open |= gate[i] < INFINITY;
+    return open;
+}
+
 // shared-memory bytes of the 1D analog kernel: table, private tallies (SMT),
 // and the per-cell gate when histories may be set aside for queries
 __host__ __device__ __forceinline__ int analog1d_smem(const CellArgs &ca, int tsz, bool smt, bool gate) {

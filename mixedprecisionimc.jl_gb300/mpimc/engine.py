@@ -330,7 +330,7 @@ def device_info():
     return {"name": name.value.decode(), "sm_count": sm.value, "cc": (ma.value, mi.value)}
 
 
-def run_batch(engines, max_steps=1 << 40, threads=16):
+def run_batch(engines, max_steps=1 << 40, threads=32):
     """Batched ensemble (imc_run_batch): runs every Engine to the end of its
     clock, the decks' kernels side by side on the GPU.  Returns (steps per
     engine, host wall seconds).  Raises ImcError naming the first failure."""
