@@ -60,7 +60,7 @@ constexpr int kNearL = 3;                    // ln(l/lmax) quantiles, near exit
 constexpr int kNearM = kNearL + kQL;         // |mu| quantiles, near exit
 constexpr int kFarL = kNearM + kQM;
 constexpr int kFarM = kFarL + kQL;
-constexpr int kTrP = kFarM + kQM;            // displacement / lmax
+constexpr int kTrP = kFarM + kQM;            // displacement / sqrt(lmax)
 constexpr int kTrM = kTrP + kQP;             // final mu'
 constexpr int kUsed = kTrM + kQM;            // 51
 static_assert(kUsed <= kOut, "heads fit the output layer");
