@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
             }
         }
     }
-    if (SMT) flush_block_tallies(ca, dep_acc);
+    if (SMT) flush_block_tallies(ca, dep_acc, true);
     if (kPause) {
         for (int off = 16; off > 0; off >>= 1) calls += __shfl_down_sync(0xFFFFFFFFu, calls, off);
         if (lane == 0 && calls) atomicAdd(&sc->surrogate_calls, calls);
@@ -333,8 +333,14 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     finish_counters<T>(sc, segs, killed, flags, emax);
 }
 
-template <class St, int BLOCK, bool SMT>
+// TM, where the flushes go: kTallyGlobal, kTallyShared (deposition and
+// census tallies block-private in shared memory) or kTallySharedDep (the
+// deposition tallies only; census energy, one flush per census particle, to
+// global memory)
+template <class St, int BLOCK, int TM>
 __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc, PBufPair bufs) {
+    constexpr bool SMT = TM != kTallyGlobal;        // deposition flushes to shared memory
+    constexpr bool RAD_SMT = TM == kTallyShared;    // census flushes to shared memory
     typedef typename St::T T;
     PBuf<St> pb(bufs.b[sc->cur]);
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -348,8 +354,8 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
     long long *dep_acc = ca.dep_acc, *rad_acc = ca.rad_acc;
     if (SMT) {
         dep_acc = tally_smem(smem_raw, table_bytes(ca, sizeof(T)));
-        rad_acc = dep_acc + 3 * (size_t)ca.K * ca.nc;
-        for (int i = threadIdx.x; i < 6 * ca.K * ca.nc; i += blockDim.x) dep_acc[i] = 0;
+        if (RAD_SMT) rad_acc = dep_acc + 3 * (size_t)ca.K * ca.nc;
+        for (int i = threadIdx.x; i < (RAD_SMT ? 6 : 3) * ca.K * ca.nc; i += blockDim.x) dep_acc[i] = 0;
     }
     for (int i = threadIdx.x; i < nc; i += blockDim.x) {
         T sa = (T)ca.sa[i], f = (T)ca.fleck[i], ss = (T)ca.ss[i];
@@ -524,7 +530,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
                 pb.E[i] = (typename St::S)E;
             }
             if (cellf != (cs & 0xFFFFFF)) pb.cs[i] = cellf | (k << 24);
-            flush_one<T, SMT>(rad_acc, k * nc + cellf, Est, b_rad, flags);
+            flush_one<T, RAD_SMT>(rad_acc, k * nc + cellf, Est, b_rad, flags);
             emax = Est > emax ? Est : emax;
             return 2;
         }
@@ -604,62 +610,80 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
             }
         }
     }
-    if (SMT) flush_block_tallies(ca, dep_acc);
+    if (SMT) flush_block_tallies(ca, dep_acc, RAD_SMT);
     finish_counters<T>(sc, segs, killed, flags, emax);
 }
 
 // Launch shape of the transport kernel.  When the table and the block's
 // private tallies fit in shared memory the kernel runs one large block per
 // SM with shared tallies (kSmtBlock32 threads for FP32 / FP16 state,
-// kSmtBlock64 for FP64);
-// otherwise tallies in global memory (kGlbBlock32 / kGlbBlock64 threads).
+// kSmtBlock64 for FP64).  In 2D, when only the table and the deposition
+// tallies fit in the opt-in maximum, the deposition tallies are shared and
+// the census flushes (one per census particle) go to global memory.
+// Otherwise every flush goes to global memory (kGlbBlock32 / kGlbBlock64
+// threads).
 constexpr int kSmemBudget = 200 * 1024;
+constexpr int kSmemOptInMax = 227 * 1024;  // sm_100-family dynamic shared memory per block
 
 TransportShape transport_shape(const CellArgs &ca, int prec) {
     TransportShape sh;
     const int tsz = prec == 0 ? 8 : 4;
     const int table = table_bytes(ca, tsz);
-    const long long tallies = 2ll * 3 * 8 * (long long)ca.K * ca.nc;
-    sh.smem_tally = table + tallies <= kSmemBudget;
-    sh.smem = sh.smem_tally ? (int)(table + tallies) : table;
-    sh.block = sh.smem_tally ? (prec == 0 ? kSmtBlock64 : kSmtBlock32) : (prec == 0 ? kGlbBlock64 : kGlbBlock32);
+    const long long dep = 3ll * 8 * (long long)ca.K * ca.nc;
+    sh.smem_tally = table + 2 * dep <= kSmemBudget;
+    sh.dep_only = !sh.smem_tally && ca.geometry == 2 && table + dep <= kSmemOptInMax;
+    sh.smem = table + (int)(sh.smem_tally ? 2 * dep : sh.dep_only ? dep : 0);
+    const bool shared = sh.smem_tally || sh.dep_only;
+    sh.block = shared ? (prec == 0 ? kSmtBlock64 : kSmtBlock32) : (prec == 0 ? kGlbBlock64 : kGlbBlock32);
     return sh;
 }
 
-template <class St, int B, bool SMT> static const void *kptr(int geometry) {
-    return geometry == 1 ? (const void *)k_transport1d<St, B, SMT, kModePlain>
-                         : (const void *)k_transport2d<St, B, SMT>;
+// the plain 1D or 2D transport kernel of one state type, block size and
+// tally mode (1D: kTallyGlobal or kTallyShared)
+template <class St, int B, int TM> static const void *kptr(int geometry) {
+    if (geometry == 1) return (const void *)k_transport1d<St, B, TM == kTallyShared, kModePlain>;
+    return (const void *)k_transport2d<St, B, TM>;
+}
+
+template <class St, int B, int TM>
+static void launch_one(const CellArgs &ca, Scalars *sc, PBufPair buf, int grid, int smem, cudaStream_t st) {
+    if (ca.geometry == 1)
+        k_transport1d<St, B, TM == kTallyShared, kModePlain><<<grid, B, smem, st>>>(ca, sc, buf, SurrWave{}, 0);
+    else k_transport2d<St, B, TM><<<grid, B, smem, st>>>(ca, sc, buf);
+}
+
+template <class St> struct StBlocks {
+    static constexpr int smt = sizeof(typename St::T) == 8 ? kSmtBlock64 : kSmtBlock32;
+    static constexpr int glb = sizeof(typename St::T) == 8 ? kGlbBlock64 : kGlbBlock32;
+};
+
+template <class St> static const void *kernel_of(const CellArgs &ca, const TransportShape &sh) {
+    if (sh.smem_tally) return kptr<St, StBlocks<St>::smt, kTallyShared>(ca.geometry);
+    if (sh.dep_only) return (const void *)k_transport2d<St, StBlocks<St>::smt, kTallySharedDep>;
+    return kptr<St, StBlocks<St>::glb, kTallyGlobal>(ca.geometry);
+}
+
+template <class St>
+static void launch_of(const CellArgs &ca, const TransportShape &sh, Scalars *sc, PBufPair buf, int grid,
+                      cudaStream_t st) {
+    if (sh.smem_tally) launch_one<St, StBlocks<St>::smt, kTallyShared>(ca, sc, buf, grid, sh.smem, st);
+    else if (sh.dep_only)
+        k_transport2d<St, StBlocks<St>::smt, kTallySharedDep><<<grid, StBlocks<St>::smt, sh.smem, st>>>(ca, sc, buf);
+    else launch_one<St, StBlocks<St>::glb, kTallyGlobal>(ca, sc, buf, grid, sh.smem, st);
 }
 
 const void *transport_kernel_ptr(const CellArgs &ca, int prec) {
     TransportShape sh = transport_shape(ca, prec);
-    if (sh.smem_tally) {
-        if (prec == 0) return kptr<StF64, kSmtBlock64, true>(ca.geometry);
-        if (prec == 1) return kptr<StF32, kSmtBlock32, true>(ca.geometry);
-        return kptr<StF16, kSmtBlock32, true>(ca.geometry);
-    }
-    if (prec == 0) return kptr<StF64, kGlbBlock64, false>(ca.geometry);
-    if (prec == 1) return kptr<StF32, kGlbBlock32, false>(ca.geometry);
-    return kptr<StF16, kGlbBlock32, false>(ca.geometry);
-}
-
-template <class St, int B, bool SMT>
-static void launch_one(const CellArgs &ca, Scalars *sc, PBufPair buf, int grid, int smem, cudaStream_t st) {
-    if (ca.geometry == 1) k_transport1d<St, B, SMT, kModePlain><<<grid, B, smem, st>>>(ca, sc, buf, SurrWave{}, 0);
-    else k_transport2d<St, B, SMT><<<grid, B, smem, st>>>(ca, sc, buf);
+    if (prec == 0) return kernel_of<StF64>(ca, sh);
+    if (prec == 1) return kernel_of<StF32>(ca, sh);
+    return kernel_of<StF16>(ca, sh);
 }
 
 void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufPair buf, int grid, cudaStream_t st) {
     TransportShape sh = transport_shape(ca, prec);
-    if (sh.smem_tally) {
-        if (prec == 0) launch_one<StF64, kSmtBlock64, true>(ca, sc, buf, grid, sh.smem, st);
-        else if (prec == 1) launch_one<StF32, kSmtBlock32, true>(ca, sc, buf, grid, sh.smem, st);
-        else launch_one<StF16, kSmtBlock32, true>(ca, sc, buf, grid, sh.smem, st);
-    } else {
-        if (prec == 0) launch_one<StF64, kGlbBlock64, false>(ca, sc, buf, grid, sh.smem, st);
-        else if (prec == 1) launch_one<StF32, kGlbBlock32, false>(ca, sc, buf, grid, sh.smem, st);
-        else launch_one<StF16, kGlbBlock32, false>(ca, sc, buf, grid, sh.smem, st);
-    }
+    if (prec == 0) launch_of<StF64>(ca, sh, sc, buf, grid, st);
+    else if (prec == 1) launch_of<StF32>(ca, sh, sc, buf, grid, st);
+    else launch_of<StF16>(ca, sh, sc, buf, grid, st);
 }
 
 // ------------------------------------------- analog passes of the surrogate transport

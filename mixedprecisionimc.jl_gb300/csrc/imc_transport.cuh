@@ -99,10 +99,11 @@ __device__ __forceinline__ long long *tally_smem(unsigned char *smem, int table)
 // Adds the block's shared tallies (deposition, then census energy, in the
 // same 3-limb layout as the global accumulators) to the global ones: limb
 // q of a slot gets its word sum plus the carries out of the limb below it.
-__device__ __forceinline__ void flush_block_tallies(const CellArgs &ca, const long long *sm) {
+// with_rad false: the block holds only the deposition tallies.
+__device__ __forceinline__ void flush_block_tallies(const CellArgs &ca, const long long *sm, bool with_rad) {
     __syncthreads();
     const int n = ca.K * ca.nc;
-    for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) {
+    for (int i = threadIdx.x; i < (with_rad ? 2 * n : n); i += blockDim.x) {
         const unsigned *w = reinterpret_cast<const unsigned *>(sm + 3 * (size_t)i);
         const int *cy = reinterpret_cast<const int *>(w + 3);
         long long *g = (i < n ? ca.dep_acc : ca.rad_acc) + 3 * (size_t)(i < n ? i : i - n);
@@ -138,6 +139,9 @@ __device__ __forceinline__ void flush_one(long long *acc, int slot, T v, int b, 
     }
     add_limbs<SMT>(acc + 3 * (size_t)slot, A);
 }
+
+// where the transport kernels add their tallies
+enum { kTallyGlobal = 0, kTallyShared = 1, kTallySharedDep = 2 };
 
 // threads per block of the shared-tally transport kernels: FP32 / FP16 state
 // and FP64 state (one block per SM: the table and the private tallies take

@@ -160,3 +160,23 @@ def test_step_parity_fp64_global_tallies(gpu_lib):
     for f in ("temp", "radenergydens", "matenergydens"):
         a, b = g.field(f), o.field(f)
         np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-9 * np.abs(b).max(), err_msg=f)
+
+
+@pytest.mark.parametrize("ysize", ["0.625", "1.0"])
+def test_step_parity_fp64_2d_large_mesh(gpu_lib, ysize):
+    """2D meshes past the shared-memory tallies: 80x50 cells (FP64 table and
+    deposition tallies in shared memory, census tallies in global memory) and
+    80x80 cells (every tally in global memory) track the oracle for three
+    steps."""
+    g, o = _pair("tiny_2d", gpu_lib, MESHTYPE="UNIFORM", XSIZE="1.0", YSIZE=ysize, DX="0.0125", DY="0.0125",
+                 NINPUT="20000", NMAX="60000")
+    assert len(g.field("temp")) == (4000 if ysize == "0.625" else 6400)
+    for _ in range(3):
+        sg, _ = g.step()
+        so, _ = o.step()
+        assert sg["n_sourced"] == so["n_sourced"]
+        assert abs(sg["n_census_out"] - so["n_census_out"]) <= max(2, 1e-4 * so["n_census_out"])
+        np.testing.assert_allclose(sg["total_energy"], so["total_energy"], rtol=1e-13)
+    for f in ("temp", "radenergydens", "matenergydens"):
+        a, b = g.field(f), o.field(f)
+        np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-9 * np.abs(b).max(), err_msg=f)
