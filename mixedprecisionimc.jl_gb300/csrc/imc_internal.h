@@ -42,6 +42,7 @@ struct Scalars {
     unsigned long long surrogate_calls;
     unsigned long long killed;         // histories this transport removed (kill, escape, cap)
     float seg_per_hist;                // segments per history of the last transport
+    unsigned long long work_next;      // transport: next chunk of the list's tail to hand out
     unsigned long long qcount[2 * kSurrRounds + 1];  // surrogate transport: ask queue of round r at 2r, resume queue at 2r + 1
     unsigned int flags;
     int b_dep, b_rad, b_lost;          // fixed-point exponents of this transport

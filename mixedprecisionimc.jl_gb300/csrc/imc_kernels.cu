@@ -353,6 +353,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_source_scan(CellArgs ca, Scala
         sc->segments = 0ull;
         sc->surrogate_calls = 0ull;
         sc->killed = 0ull;
+        sc->work_next = 0ull;
         for (int r = 0; r <= 2 * kSurrRounds; ++r) sc->qcount[r] = 0ull;
         sc->b_dep = fix_exponent(emax / ca.vol_min);
         sc->b_lost = fix_exponent(emax);
@@ -907,6 +908,7 @@ __global__ void k_prepare_transport(CellArgs ca, Scalars *sc) {
     sc->segments = 0ull;
     sc->surrogate_calls = 0ull;
     sc->killed = 0ull;
+    sc->work_next = 0ull;
     for (int r = 0; r <= 2 * kSurrRounds; ++r) sc->qcount[r] = 0ull;
     sc->n_census_in = sc->n_census;
     sc->n_sourced = 0;

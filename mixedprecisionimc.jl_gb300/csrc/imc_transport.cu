@@ -254,13 +254,23 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         // kRefillSegments segments each): each lane walks one history to its
         // end, and the warp moves on together to 32 consecutive entries, so
         // every load and store of the list is coalesced.
-        for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+        auto walk = [&](long long e) {
             int cs_now;
-            if (!load(e, cs_now, t, x, mu, E, E0, i, cs)) continue;
+            if (!load(e, cs_now, t, x, mu, E, E0, i, cs)) return;
             start(cs_now);
             int end;
             do end = segment(); while (!end);
             finish(end);
+        };
+        // the queue of a resume pass by grid stride; the list by grid stride
+        // and then tail chunks (kTailChunk)
+        const long long n_static = kFromQueue ? n : static_share(n, stride);
+        for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n_static; e += stride) walk(e);
+        if (!kFromQueue) {
+            for (long long base = next_tail_chunk(&sc->work_next, n_static); base < n;
+                 base = next_tail_chunk(&sc->work_next, n_static))
+                for (int r = 0; r < kTailChunk; r += 32)
+                    if (base + r + lane < n) walk(base + r + lane);
         }
     } else {
         // Long histories of unequal length: each lane starts the next history
@@ -546,14 +556,21 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
     };
     if (sc->seg_per_hist < kRefillSegments) {
         // short histories: one history per lane to its end (see k_transport1d)
-        for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
-            if (!load(e, cs, t, xp, yp, vx, vy, E, E0)) continue;
+        auto walk = [&](long long e) {
+            if (!load(e, cs, t, xp, yp, vx, vy, E, E0)) return;
             i = e;
             start();
             int end;
             do end = segment(); while (!end);
             finish(end);
-        }
+        };
+        const long long n_static = static_share(n, stride);
+        for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n_static; e += stride) walk(e);
+        const int lane = threadIdx.x & 31;
+        for (long long base = next_tail_chunk(&sc->work_next, n_static); base < n;
+             base = next_tail_chunk(&sc->work_next, n_static))
+            for (int r = 0; r < kTailChunk; r += 32)
+                if (base + r + lane < n) walk(base + r + lane);
     } else {
         // long histories: lanes refill from 32-entry chunks (see k_transport1d)
         const int lane = threadIdx.x & 31;
