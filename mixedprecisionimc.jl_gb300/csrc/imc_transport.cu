@@ -281,7 +281,16 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         const unsigned lt = (1u << lane) - 1u;
         const long long nchunks = (n + 31) / 32;
         const long long cstride = (long long)gridDim.x * (BLOCK / 32);
+        // chunks by grid stride over the first 7/8, then (list passes) from
+        // the counter, as in the short-history schedule
+        const long long nstat = kFromQueue ? nchunks : static_share(nchunks, cstride);
         long long chunk = (long long)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
+        if (chunk >= nstat && !kFromQueue) chunk = nstat + warp_counter_next(&sc->work_next);
+        auto advance = [&]() {
+            if (chunk + cstride < nstat) chunk += cstride;
+            else if (kFromQueue) chunk = nchunks;
+            else chunk = nstat + warp_counter_next(&sc->work_next);
+        };
         int p_now = -1, p_cs = 0;  // prefetched entry (p_now -1: none / dead)
         long long p_i = 0;
         T p_t = (T)0, p_x = (T)0, p_mu = (T)0, p_E = (T)0, p_E0 = (T)0;
@@ -319,7 +328,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
                 const int nidle = __popc(idle);
                 pos += nidle < avail ? nidle : avail;
                 if (pos >= 32) {
-                    chunk += cstride;
+                    advance();
                     more = chunk < nchunks;
                     pos = 0;
                     if (more) prefetch();
@@ -577,7 +586,14 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
         const unsigned lt = (1u << lane) - 1u;
         const long long nchunks = (n + 31) / 32;
         const long long cstride = (long long)gridDim.x * (BLOCK / 32);
+        // chunks by grid stride over the first 7/8, then from the counter
+        const long long nstat = static_share(nchunks, cstride);
         long long chunk = (long long)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
+        if (chunk >= nstat) chunk = nstat + warp_counter_next(&sc->work_next);
+        auto advance = [&]() {
+            if (chunk + cstride < nstat) chunk += cstride;
+            else chunk = nstat + warp_counter_next(&sc->work_next);
+        };
         int p_cs = -1;
         T p_t = (T)0, p_x = (T)0, p_y = (T)0, p_vx = (T)0, p_vy = (T)0, p_E = (T)0, p_E0 = (T)0;
         auto prefetch = [&]() {
@@ -611,7 +627,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
                 const int nidle = __popc(idle);
                 pos += nidle < avail ? nidle : avail;
                 if (pos >= 32) {
-                    chunk += cstride;
+                    advance();
                     more = chunk < nchunks;
                     pos = 0;
                     if (more) prefetch();

@@ -140,21 +140,25 @@ __device__ __forceinline__ void flush_one(long long *acc, int slot, T v, int b, 
     add_limbs<SMT>(acc + 3 * (size_t)slot, A);
 }
 
-// Work split of the short-history schedule over the particle list: the first
-// 7/8 (rounded down to whole grid strides) by grid stride, the rest in
-// kTailChunk-entry warp chunks from a counter (Scalars::work_next), so the
-// blocks (one per SM) run out of work together instead of the last ones
-// holding a few SMs while the others wait at the final barrier.
+// Work split of the transport over the particle list: the first 7/8 (rounded
+// down to whole grid strides) by grid stride, the rest from a counter
+// (Scalars::work_next) -- kTailChunk-entry warp chunks in the short-history
+// schedule, 32-entry chunks in the refill schedule -- so the blocks (one per
+// SM) run out of work together instead of the last ones holding a few SMs
+// while the others wait at the final barrier.
 constexpr int kTailChunk = 128;
 __host__ __device__ __forceinline__ long long static_share(long long n, long long stride) {
     return (n - n / 8) / stride * stride;
 }
-// the next tail chunk's first entry (warp-uniform; every lane of the warp calls)
-__device__ __forceinline__ long long next_tail_chunk(unsigned long long *counter, long long n_static) {
+// the counter's next value for the warp (warp-uniform; every lane calls)
+__device__ __forceinline__ long long warp_counter_next(unsigned long long *counter) {
     unsigned long long c = 0;
     if ((threadIdx.x & 31) == 0) c = atomicAdd(counter, 1ull);
-    c = __shfl_sync(0xFFFFFFFFu, c, 0);
-    return n_static + (long long)c * kTailChunk;
+    return (long long)__shfl_sync(0xFFFFFFFFu, c, 0);
+}
+// the next tail chunk's first entry
+__device__ __forceinline__ long long next_tail_chunk(unsigned long long *counter, long long n_static) {
+    return n_static + warp_counter_next(counter) * kTailChunk;
 }
 
 // where the transport kernels add their tallies
