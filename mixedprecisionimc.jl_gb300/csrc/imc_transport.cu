@@ -3,9 +3,10 @@
 //   k_transport1d <- Transport.MC   (src/imc_transport.jl:13-210)
 //   k_transport2d <- Transport.MC2D (src/imc_transport.jl:483-732)
 //
-// A persistent grid walks the particle list with a grid stride, so every
-// warp loads 32 consecutive particles (coalesced structure-of-arrays loads)
-// and keeps the whole history in registers: each particle's state is read
+// A persistent grid walks the particle list in chunks of consecutive entries
+// that warps take from a counter, so every warp loads 32 consecutive
+// particles (coalesced structure-of-arrays loads) and the blocks run out of
+// work together; a history stays in registers: each particle's state is read
 // once and written once per step.  The per-cell transport table (sigma_a*f,
 // effective scatter, face widths) is built in shared memory by every block.
 //
@@ -262,14 +263,14 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
             do end = segment(); while (!end);
             finish(end);
         };
-        // the queue of a resume pass by grid stride; the list by grid stride
-        // and then tail chunks (kTailChunk)
-        const long long n_static = kFromQueue ? n : static_share(n, stride);
-        for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n_static; e += stride) walk(e);
-        if (!kFromQueue) {
-            for (long long base = next_tail_chunk(&sc->work_next, n_static); base < n;
-                 base = next_tail_chunk(&sc->work_next, n_static))
-                for (int r = 0; r < kTailChunk; r += 32)
+        // the queue of a resume pass by grid stride, the list in chunks from
+        // the counter
+        if (kFromQueue) {
+            for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) walk(e);
+        } else {
+            for (long long base = warp_counter_next(&sc->work_next) * kListChunk; base < n;
+                 base = warp_counter_next(&sc->work_next) * kListChunk)
+                for (int r = 0; r < kListChunk; r += 32)
                     if (base + r + lane < n) walk(base + r + lane);
         }
     } else {
@@ -281,16 +282,11 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         const unsigned lt = (1u << lane) - 1u;
         const long long nchunks = (n + 31) / 32;
         const long long cstride = (long long)gridDim.x * (BLOCK / 32);
-        // chunks by grid stride over the first 7/8, then (list passes) from
-        // the counter, as in the short-history schedule
-        const long long nstat = kFromQueue ? nchunks : static_share(nchunks, cstride);
-        long long chunk = (long long)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
-        if (chunk >= nstat && !kFromQueue) chunk = nstat + warp_counter_next(&sc->work_next);
-        auto advance = [&]() {
-            if (chunk + cstride < nstat) chunk += cstride;
-            else if (kFromQueue) chunk = nchunks;
-            else chunk = nstat + warp_counter_next(&sc->work_next);
-        };
+        // chunks of a resume pass's queue by grid stride, of the list from
+        // the counter
+        long long chunk = kFromQueue ? (long long)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5)
+                                     : warp_counter_next(&sc->work_next);
+        auto advance = [&]() { chunk = kFromQueue ? chunk + cstride : warp_counter_next(&sc->work_next); };
         int p_now = -1, p_cs = 0;  // prefetched entry (p_now -1: none / dead)
         long long p_i = 0;
         T p_t = (T)0, p_x = (T)0, p_mu = (T)0, p_E = (T)0, p_E0 = (T)0;
@@ -400,7 +396,6 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
     unsigned long long segs = 0, killed = 0;
     unsigned flags = 0;
     T emax = (T)0;
-    const long long stride = (long long)gridDim.x * blockDim.x;
     // Lane state of the history in flight.
     long long i = 0;
     int cs = 0, xi = 0, yi = 0, k = 0, acc_cell = 0;
@@ -573,27 +568,20 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
             do end = segment(); while (!end);
             finish(end);
         };
-        const long long n_static = static_share(n, stride);
-        for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n_static; e += stride) walk(e);
+        // the list in chunks from the counter
         const int lane = threadIdx.x & 31;
-        for (long long base = next_tail_chunk(&sc->work_next, n_static); base < n;
-             base = next_tail_chunk(&sc->work_next, n_static))
-            for (int r = 0; r < kTailChunk; r += 32)
+        for (long long base = warp_counter_next(&sc->work_next) * kListChunk; base < n;
+             base = warp_counter_next(&sc->work_next) * kListChunk)
+            for (int r = 0; r < kListChunk; r += 32)
                 if (base + r + lane < n) walk(base + r + lane);
     } else {
         // long histories: lanes refill from 32-entry chunks (see k_transport1d)
         const int lane = threadIdx.x & 31;
         const unsigned lt = (1u << lane) - 1u;
         const long long nchunks = (n + 31) / 32;
-        const long long cstride = (long long)gridDim.x * (BLOCK / 32);
-        // chunks by grid stride over the first 7/8, then from the counter
-        const long long nstat = static_share(nchunks, cstride);
-        long long chunk = (long long)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
-        if (chunk >= nstat) chunk = nstat + warp_counter_next(&sc->work_next);
-        auto advance = [&]() {
-            if (chunk + cstride < nstat) chunk += cstride;
-            else chunk = nstat + warp_counter_next(&sc->work_next);
-        };
+        // chunks from the counter
+        long long chunk = warp_counter_next(&sc->work_next);
+        auto advance = [&]() { chunk = warp_counter_next(&sc->work_next); };
         int p_cs = -1;
         T p_t = (T)0, p_x = (T)0, p_y = (T)0, p_vx = (T)0, p_vy = (T)0, p_E = (T)0, p_E0 = (T)0;
         auto prefetch = [&]() {
