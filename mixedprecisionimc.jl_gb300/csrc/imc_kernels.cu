@@ -594,19 +594,6 @@ __global__ void __launch_bounds__(1024) k_compact_scan(Scalars *sc, const long l
     }
 }
 
-// Copies one field of a tile: coalesced load of the tile into shared memory,
-// then coalesced stores of the survivors in order (src_idx[j] is the tile
-// position of the j-th survivor).
-template <class V>
-__device__ __forceinline__ void scatter_field(const V *src, V *dst, long long base, int tile_n, long long out,
-                                              int cnt, const unsigned short *src_idx, unsigned char *stage) {
-    V *st = reinterpret_cast<V *>(stage);
-    for (int i = threadIdx.x; i < tile_n; i += blockDim.x) st[i] = src[base + i];
-    __syncthreads();
-    for (int j = threadIdx.x; j < cnt; j += blockDim.x) dst[out + j] = st[src_idx[j]];
-    __syncthreads();
-}
-
 template <class St>
 __global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(int geometry, const Scalars *sc,
                                                                      const long long *tile_off, PBufPair bufs,
@@ -614,7 +601,6 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(int geometr
     if (!sc->compact_now) return;
     PBuf<St> src(bufs.b[sc->compact_src]), dst(bufs.b[sc->compact_src ^ 1]);
     __shared__ unsigned short src_idx[kCompactTile];
-    __shared__ __align__(16) unsigned char stage[kCompactTile * 8];
     __shared__ int wt[kCompactThreads / 32];
     __shared__ int s_tot;
     const long long n = *n_before;
@@ -658,17 +644,27 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(int geometr
     __syncthreads();
     const int cnt = run;
     const long long out = tile_off[blockIdx.x];
-    scatter_field(src.t, dst.t, base, tile_n, out, cnt, src_idx, stage);
-    scatter_field(src.x, dst.x, base, tile_n, out, cnt, src_idx, stage);
-    scatter_field(src.ux, dst.ux, base, tile_n, out, cnt, src_idx, stage);
-    if (geometry == 2) {
-        scatter_field(src.y, dst.y, base, tile_n, out, cnt, src_idx, stage);
-        scatter_field(src.uy, dst.uy, base, tile_n, out, cnt, src_idx, stage);
+    // Every field of a survivor in one pass: stores coalesced, loads gathered
+    // from the tile (whole sectors when most entries survive; when most are
+    // holes, only the sectors that hold a survivor), all fields' loads of a
+    // survivor in flight together.
+    for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+        const long long f = base + src_idx[j], d = out + j;
+        const auto t = src.t[f], x = src.x[f], ux = src.ux[f];
+        const auto E = src.E[f];
+        const auto E0 = src.E0[f];
+        const int cs = src.cs[f];
+        if (geometry == 2) {
+            const auto y = src.y[f], uy = src.uy[f];
+            dst.y[d] = y;
+            dst.uy[d] = uy;
+        }
+        dst.t[d] = t; dst.x[d] = x; dst.ux[d] = ux;
+        dst.E[d] = E;
+        dst.E0[d] = E0;
+        dst.cs[d] = cs;
+        dst.alive[d] = 1;
     }
-    scatter_field(src.E, dst.E, base, tile_n, out, cnt, src_idx, stage);
-    scatter_field(src.E0, dst.E0, base, tile_n, out, cnt, src_idx, stage);
-    scatter_field(src.cs, dst.cs, base, tile_n, out, cnt, src_idx, stage);
-    for (int j = threadIdx.x; j < cnt; j += blockDim.x) dst.alive[out + j] = 1;
 }
 
 // Before compaction: the list length (for the scatter) and whether this step
