@@ -78,7 +78,6 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     unsigned long long segs = 0, calls = 0, killed = 0;
     unsigned flags = 0;
     T emax = (T)0;
-    const long long stride = (long long)gridDim.x * blockDim.x;
     // Lane state of the history in flight (cs: as stored in the list; the
     // current cell and scale are cell, k).
     long long i = 0;
@@ -263,16 +262,11 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
             do end = segment(); while (!end);
             finish(end);
         };
-        // the queue of a resume pass by grid stride, the list in chunks from
-        // the counter
-        if (kFromQueue) {
-            for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) walk(e);
-        } else {
-            for (long long base = warp_counter_next(&sc->work_next) * kListChunk; base < n;
-                 base = warp_counter_next(&sc->work_next) * kListChunk)
-                for (int r = 0; r < kListChunk; r += 32)
-                    if (base + r + lane < n) walk(base + r + lane);
-        }
+        // the list (or a resume pass's queue) in chunks from the counter
+        for (long long base = warp_counter_next(&sc->work_next) * kListChunk; base < n;
+             base = warp_counter_next(&sc->work_next) * kListChunk)
+            for (int r = 0; r < kListChunk; r += 32)
+                if (base + r + lane < n) walk(base + r + lane);
     } else {
         // Long histories of unequal length: each lane starts the next history
         // as soon as its current one ends.  The warp reads the entries in
@@ -281,12 +275,9 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         // register shuffles.
         const unsigned lt = (1u << lane) - 1u;
         const long long nchunks = (n + 31) / 32;
-        const long long cstride = (long long)gridDim.x * (BLOCK / 32);
-        // chunks of a resume pass's queue by grid stride, of the list from
-        // the counter
-        long long chunk = kFromQueue ? (long long)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5)
-                                     : warp_counter_next(&sc->work_next);
-        auto advance = [&]() { chunk = kFromQueue ? chunk + cstride : warp_counter_next(&sc->work_next); };
+        // chunks of the list (or of a resume pass's queue) from the counter
+        long long chunk = warp_counter_next(&sc->work_next);
+        auto advance = [&]() { chunk = warp_counter_next(&sc->work_next); };
         int p_now = -1, p_cs = 0;  // prefetched entry (p_now -1: none / dead)
         long long p_i = 0;
         T p_t = (T)0, p_x = (T)0, p_mu = (T)0, p_E = (T)0, p_E0 = (T)0;

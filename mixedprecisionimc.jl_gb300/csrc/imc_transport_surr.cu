@@ -223,6 +223,9 @@ template <class St>
 __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scalars *sc, PBufPair bufs, SurrWave w,
                                                                int round) {
     typedef float T;
+    // the resume pass after this one takes its queue chunks from the work
+    // counter, which the pass before this one has finished using
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->work_next = 0ull;
     const long long n = (long long)sc->qcount[2 * round];
     if (n == 0) return;
     PBuf<St> pb(bufs.b[sc->cur]);
