@@ -38,6 +38,7 @@ struct Scalars {
     long long birth_base;              // list index of this step's first birth
     long long n_sourced;
     double n_source;                   // particle budget of this step
+    double src_group[6];               // sourcing: energy/escale sum of each slot group
     unsigned long long segments;
     unsigned long long surrogate_calls;
     unsigned long long killed;         // histories this transport removed (kill, escape, cap)

@@ -216,15 +216,19 @@ __device__ __forceinline__ double warp_sum_partials(const double *part, int nb, 
     return __shfl_sync(0xFFFFFFFFu, d.val(), 0);
 }
 
-// Total energy (src/imc_sourcing.jl:121) and particle budget (:132-136).
-// Six warps, one per slot group.
-__global__ void __launch_bounds__(192) k_source_total(CellArgs ca, Scalars *sc) {
-    __shared__ double g[6];
-    const int warp = threadIdx.x >> 5;
-    double v = warp_sum_partials(ca.part_src, ca.nblk_slot, 6, warp);
-    if ((threadIdx.x & 31) == 0) g[warp] = v;
-    __syncthreads();
-    if (threadIdx.x != 0) return;
+// Sums of the slot groups (src/imc_sourcing.jl:121): one one-warp block per
+// group, so each sum has an SM's FP64 pipe to itself (1D needs only the body
+// and radiation-source groups; its two surfaces are added directly).
+__global__ void __launch_bounds__(32) k_source_total(CellArgs ca, Scalars *sc) {
+    const double v = warp_sum_partials(ca.part_src, ca.nblk_slot, 6, blockIdx.x);
+    if (threadIdx.x == 0) sc->src_group[blockIdx.x] = v;
+}
+
+// Total energy (src/imc_sourcing.jl:121) and particle budget (:132-136) from
+// the group sums, in a fixed order: every block of k_source_counts computes
+// the same values.
+__device__ __forceinline__ void source_total(const CellArgs &ca, const Scalars *sc, double &E, double &n_source) {
+    const double *g = sc->src_group;
     double e_surface;
     if (ca.geometry == 1) {
         e_surface = ca.slot_q[0] + ca.slot_q[1];
@@ -235,24 +239,28 @@ __global__ void __launch_bounds__(192) k_source_total(CellArgs ca, Scalars *sc) 
         e_surface += g[4];
         e_surface += g[5];
     }
-    const double E = g[0] + g[1] + e_surface;
+    E = g[0] + g[1] + e_surface;
     const long long n_census = sc->n_census;
-    double n_source = (double)ca.n_input;
+    n_source = (double)ca.n_input;
     if (ca.n_input + n_census > ca.n_max) {
         double lenN = ca.geometry == 1 ? 1.0 : 2.0;
         n_source = fmax(ca.cellmin, (double)(ca.n_max - n_census) - lenN - 1.0);
     }
-    sc->totalenergy = E;
-    sc->n_source = n_source;
-    if (!((E > 0.0) && isfinite(E))) sc->flags |= 1u << 4;
 }
 
-// Births per slot (src/imc_sourcing.jl:138-157) and per-particle energy.
+// Births per slot (src/imc_sourcing.jl:138-157) and per-particle energy;
+// block 0 also records the step's total energy and budget.
 __global__ void __launch_bounds__(kCellThreads) k_source_counts(CellArgs ca, Scalars *sc) {
     __shared__ double wm[kCellThreads / 32];
     const int ns = nsurf_slots(ca), nc = ca.nc;
-    const double E = sc->totalenergy, n_source = sc->n_source;
+    double E, n_source;
+    source_total(ca, sc, E, n_source);
     const bool ok = (E > 0.0) && isfinite(E);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        sc->totalenergy = E;
+        sc->n_source = n_source;
+        if (!ok) atomicOr(&sc->flags, 1u << 4);
+    }
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     double my = 0.0;
     if (q < ca.nslots) {
@@ -503,7 +511,7 @@ void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufPair buf, int 
     auto slots = ca.geometry == 1 ? (ca.sel_prec == 2 ? k_source_slots<1, 2> : ca.sel_prec == 1 ? k_source_slots<1, 1> : k_source_slots<1, 0>)
                                   : (ca.sel_prec == 2 ? k_source_slots<2, 2> : ca.sel_prec == 1 ? k_source_slots<2, 1> : k_source_slots<2, 0>);
     slots<<<nb, kCellThreads, 0, st>>>(ca, sc);
-    k_source_total<<<1, 192, 0, st>>>(ca, sc);
+    k_source_total<<<ca.geometry == 1 ? 2 : 6, 32, 0, st>>>(ca, sc);
     k_source_counts<<<nb, kCellThreads, 0, st>>>(ca, sc);
     k_source_scan<<<1, kPlanThreads, 0, st>>>(ca, sc);
     if (prec == 0) k_source_emit<StF64><<<grid, 256, 0, st>>>(ca, sc, buf);
