@@ -951,8 +951,9 @@ struct StateHeader {
     int64_t n_particles;
     double t, dt;
     int64_t step, finished, tot_segments, tot_histories, tot_calls;
+    int64_t scalars_bytes;  // the device scalars' layout must match too
 };
-constexpr int32_t kStateVersion = 1;
+constexpr int32_t kStateVersion = 2;
 
 struct Piece {
     void *dev;
@@ -998,6 +999,7 @@ int imc_save_state(const ImcHandle *hc, void *buf, size_t *len) {
     hd.version = kStateVersion; hd.prec = h->prec; hd.geometry = h->geometry; hd.nx = h->nx; hd.ny = h->ny; hd.K = h->K;
     hd.n_particles = n; hd.t = h->t; hd.dt = h->dt; hd.step = h->step; hd.finished = h->finished ? 1 : 0;
     hd.tot_segments = h->tot_segments; hd.tot_histories = h->tot_histories; hd.tot_calls = h->tot_calls;
+    hd.scalars_bytes = (int64_t)sizeof(Scalars);
     std::memcpy(o, &hd, sizeof hd); o += sizeof hd;
     std::memcpy(o, &sc, sizeof sc); o += sizeof sc;
     for (auto &p : cells) { CK(h, hcopy(h, o, p.dev, p.bytes, cudaMemcpyDeviceToHost)); o += p.bytes; }
@@ -1011,7 +1013,8 @@ int imc_load_state(ImcHandle *h, const void *buf, size_t len) {
     const unsigned char *in = static_cast<const unsigned char *>(buf);
     StateHeader hd;
     std::memcpy(&hd, in, sizeof hd); in += sizeof hd;
-    if (std::memcmp(hd.magic, "IMCSTATE", 8) != 0 || hd.version != kStateVersion)
+    if (std::memcmp(hd.magic, "IMCSTATE", 8) != 0 || hd.version != kStateVersion ||
+        hd.scalars_bytes != (int64_t)sizeof(Scalars))
         return fail(h, IMC_ERR_INVALID_ARG, "not a state blob of this library version");
     if (hd.prec != h->prec || hd.geometry != h->geometry || hd.nx != h->nx || hd.ny != h->ny || hd.K != h->K)
         return fail(h, IMC_ERR_INVALID_ARG, "state blob of another deck (precision, geometry, mesh or scales)");
