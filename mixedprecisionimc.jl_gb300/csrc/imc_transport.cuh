@@ -144,9 +144,10 @@ __device__ __forceinline__ void flush_one(long long *acc, int slot, T v, int b, 
 // queue): warps take chunks in order from a counter (Scalars::work_next,
 // zeroed before each transport and by each query pass) -- kListChunk-entry
 // chunks in the short-history schedule, 32-entry chunks in the refill
-// schedule -- so the blocks (one per SM) run out of work together.  Measured against a fixed grid stride over 7/8 of the list
-// with the rest from the counter: the same on the slab (+0.7 %), 29 % faster
-// transport on the 2D channel, whose history costs vary along the list.
+// schedule -- so the blocks (one per SM) run out of work together.  Measured
+// against a fixed grid stride over 7/8 of the list with the rest from the
+// counter: the same on the slab (+0.7 %), 29 % faster transport on the 2D
+// channel, whose history costs vary along the list.
 constexpr int kListChunk = 128;
 // the counter's next value for the warp (warp-uniform; every lane calls)
 __device__ __forceinline__ long long warp_counter_next(unsigned long long *counter) {
