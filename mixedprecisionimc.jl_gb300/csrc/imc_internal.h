@@ -109,7 +109,7 @@ void launch_update(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 void launch_source(const CellArgs &ca, Scalars *sc, int prec, PBufPair bufs, int grid, cudaStream_t st);
 struct TransportShape {
     bool smem_tally;  // block-private tallies in shared memory
-    bool dep_only;    // 2D: only the deposition tallies in shared memory
+    bool dep_only;    // only the deposition tallies in shared memory
     int smem;         // dynamic shared memory bytes
     int block;        // threads per block
 };

@@ -34,9 +34,13 @@ constexpr float kRefillSegments = 3.0f;
 // pass walks everything to its end.
 enum { kModePlain = 0, kModeList = 1, kModeResume = 2, kModeResumeLast = 3 };
 
-template <class St, int BLOCK, bool SMT, int MODE>
+// TM: where the flushes go (kTallyGlobal, kTallyShared, or kTallySharedDep:
+// deposition tallies shared, census tallies global; the plain pass only)
+template <class St, int BLOCK, int TM, int MODE>
 __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc, PBufPair bufs, SurrWave w,
                                                        int round) {
+    constexpr bool SMT = TM != kTallyGlobal;      // deposition flushes to shared memory
+    constexpr bool RAD_SMT = TM == kTallyShared;  // census flushes to shared memory
     typedef typename St::T T;
     typedef SegMath<T> M;
     constexpr bool kFromQueue = MODE == kModeResume || MODE == kModeResumeLast;
@@ -53,11 +57,12 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     long long *dep_acc = ca.dep_acc, *rad_acc = ca.rad_acc;
     if (SMT) {
         dep_acc = tally_smem(smem_raw, table_bytes(ca, sizeof(T)));
-        rad_acc = dep_acc + 3 * (size_t)ca.K * ca.nc;
-        for (int i = threadIdx.x; i < 6 * ca.K * ca.nc; i += blockDim.x) dep_acc[i] = 0;
+        if (RAD_SMT) rad_acc = dep_acc + 3 * (size_t)ca.K * ca.nc;
+        for (int i = threadIdx.x; i < (RAD_SMT ? 6 : 3) * ca.K * ca.nc; i += blockDim.x) dep_acc[i] = 0;
     }
+    static_assert(TM != kTallySharedDep || MODE == kModePlain, "deposition-only tallies: plain pass only");
     const T endsteptime = (T)sc->dt;
-    float *gate = reinterpret_cast<float *>(smem_raw + analog1d_smem(ca, sizeof(T), SMT, false));
+    float *gate = reinterpret_cast<float *>(smem_raw + analog1d_smem(ca, sizeof(T), RAD_SMT, false));
     for (int i = threadIdx.x; i < N; i += blockDim.x) tab[i] = make_tab1<T>(ca.sa[i], ca.fleck[i], ca.ss[i], ca.dx[i], ds);
     if (kPause) fill_gate<T>(ca, gate, ds, c, endsteptime);
     // the barrier after the table; with the gate, also whether any cell's
@@ -226,7 +231,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
                             pb.E[i] = (typename St::S)E;
                         }
                         if (cell != (cs & 0xFFFFFF)) pb.cs[i] = cell | (k << 24);
-                        flush_one<T, SMT>(rad_acc, k * nc + cell, Est, b_rad, flags);
+                        flush_one<T, RAD_SMT>(rad_acc, k * nc + cell, Est, b_rad, flags);
                         emax = Est > emax ? Est : emax;
                         end = 2;
                     }
@@ -331,7 +336,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
             }
         }
     }
-    if (SMT) flush_block_tallies(ca, dep_acc, true);
+    if (SMT) flush_block_tallies(ca, dep_acc, RAD_SMT);
     if (kPause) {
         for (int off = 16; off > 0; off >>= 1) calls += __shfl_down_sync(0xFFFFFFFFu, calls, off);
         if (lane == 0 && calls) atomicAdd(&sc->surrogate_calls, calls);
@@ -629,9 +634,10 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
 // Launch shape of the transport kernel.  When the table and the block's
 // private tallies fit in shared memory the kernel runs one large block per
 // SM with shared tallies (kSmtBlock32 threads for FP32 / FP16 state,
-// kSmtBlock64 for FP64).  In 2D, when only the table and the deposition
-// tallies fit in the opt-in maximum, the deposition tallies are shared and
-// the census flushes (one per census particle) go to global memory.
+// kSmtBlock64 for FP64).  When only the table and the deposition tallies fit
+// in the opt-in maximum, the deposition tallies are shared and the census
+// flushes (one per census particle) go to global memory (the analog passes
+// of the surrogate transport then keep every tally global).
 // Otherwise every flush goes to global memory (kGlbBlock32 / kGlbBlock64
 // threads).
 constexpr int kSmemBudget = 200 * 1024;
@@ -643,7 +649,7 @@ TransportShape transport_shape(const CellArgs &ca, int prec) {
     const int table = table_bytes(ca, tsz);
     const long long dep = 3ll * 8 * (long long)ca.K * ca.nc;
     sh.smem_tally = table + 2 * dep <= kSmemBudget;
-    sh.dep_only = !sh.smem_tally && ca.geometry == 2 && table + dep <= kSmemOptInMax;
+    sh.dep_only = !sh.smem_tally && table + dep <= kSmemOptInMax;
     sh.smem = table + (int)(sh.smem_tally ? 2 * dep : sh.dep_only ? dep : 0);
     const bool shared = sh.smem_tally || sh.dep_only;
     sh.block = shared ? (prec == 0 ? kSmtBlock64 : kSmtBlock32) : (prec == 0 ? kGlbBlock64 : kGlbBlock32);
@@ -651,16 +657,15 @@ TransportShape transport_shape(const CellArgs &ca, int prec) {
 }
 
 // the plain 1D or 2D transport kernel of one state type, block size and
-// tally mode (1D: kTallyGlobal or kTallyShared)
+// tally mode
 template <class St, int B, int TM> static const void *kptr(int geometry) {
-    if (geometry == 1) return (const void *)k_transport1d<St, B, TM == kTallyShared, kModePlain>;
+    if (geometry == 1) return (const void *)k_transport1d<St, B, TM, kModePlain>;
     return (const void *)k_transport2d<St, B, TM>;
 }
 
 template <class St, int B, int TM>
 static void launch_one(const CellArgs &ca, Scalars *sc, PBufPair buf, int grid, int smem, cudaStream_t st) {
-    if (ca.geometry == 1)
-        k_transport1d<St, B, TM == kTallyShared, kModePlain><<<grid, B, smem, st>>>(ca, sc, buf, SurrWave{}, 0);
+    if (ca.geometry == 1) k_transport1d<St, B, TM, kModePlain><<<grid, B, smem, st>>>(ca, sc, buf, SurrWave{}, 0);
     else k_transport2d<St, B, TM><<<grid, B, smem, st>>>(ca, sc, buf);
 }
 
@@ -671,7 +676,7 @@ template <class St> struct StBlocks {
 
 template <class St> static const void *kernel_of(const CellArgs &ca, const TransportShape &sh) {
     if (sh.smem_tally) return kptr<St, StBlocks<St>::smt, kTallyShared>(ca.geometry);
-    if (sh.dep_only) return (const void *)k_transport2d<St, StBlocks<St>::smt, kTallySharedDep>;
+    if (sh.dep_only) return kptr<St, StBlocks<St>::smt, kTallySharedDep>(ca.geometry);
     return kptr<St, StBlocks<St>::glb, kTallyGlobal>(ca.geometry);
 }
 
@@ -679,8 +684,7 @@ template <class St>
 static void launch_of(const CellArgs &ca, const TransportShape &sh, Scalars *sc, PBufPair buf, int grid,
                       cudaStream_t st) {
     if (sh.smem_tally) launch_one<St, StBlocks<St>::smt, kTallyShared>(ca, sc, buf, grid, sh.smem, st);
-    else if (sh.dep_only)
-        k_transport2d<St, StBlocks<St>::smt, kTallySharedDep><<<grid, StBlocks<St>::smt, sh.smem, st>>>(ca, sc, buf);
+    else if (sh.dep_only) launch_one<St, StBlocks<St>::smt, kTallySharedDep>(ca, sc, buf, grid, sh.smem, st);
     else launch_one<St, StBlocks<St>::glb, kTallyGlobal>(ca, sc, buf, grid, sh.smem, st);
 }
 

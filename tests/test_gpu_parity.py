@@ -147,11 +147,15 @@ def test_bit_reproducible(gpu_lib):
         np.testing.assert_array_equal(x, y)
 
 
-def test_step_parity_fp64_global_tallies(gpu_lib):
-    """A 4000-cell slab: the per-cell table and tallies no longer fit in
-    shared memory, so the kernels add their exact tallies in global memory
-    (warp-aggregated); three steps still track the oracle."""
-    g, o = _pair("c1_slab", gpu_lib, DX="0.0025", NINPUT="20000", NMAX="200000")
+@pytest.mark.parametrize("dx", ["0.0025", "0.002"])
+def test_step_parity_fp64_large_slab(gpu_lib, dx):
+    """Slabs past the shared-memory tallies: 4000 cells (FP64 table and
+    deposition tallies in shared memory, census tallies in global memory) and
+    5000 cells (every tally in global memory, warp-combined; the FP64 table
+    alone still fits, up to ~7000 cells); three steps still track the
+    oracle."""
+    g, o = _pair("c1_slab", gpu_lib, DX=dx, NINPUT="20000", NMAX="200000")
+    assert len(g.field("temp")) == (4000 if dx == "0.0025" else 5000)
     for _ in range(3):
         sg, _ = g.step()
         so, _ = o.step()
