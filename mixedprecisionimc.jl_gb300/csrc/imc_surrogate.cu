@@ -4,7 +4,7 @@
 //   k_surr_datagen  the analog in-cell walk (the physics of Transport.MC inside
 //                   one cell, src/imc_transport.jl:72-193, in mean free paths)
 //                   from random walk states; its outcomes are the training
-//                   targets and, in the tests, the judge of the sampled ones
+//                   targets and, in the tests, the yardstick of the sampled ones
 //   k_surr_grad     forward + backward of a 64-sample slice in FP32: the loss
 //                   (cross entropy of the outcome + pinball losses of the
 //                   outcome's quantile heads) and per-block weight gradients
