@@ -12,7 +12,17 @@ for p in (PKG, os.path.join(REPO, "oracle")):
         sys.path.insert(0, p)
 
 DECKS = os.path.join(REPO, "tests", "golden", "decks")
-REFERENCE = "/root/reference"
+# Root of a reference checkout, for the tests that read its files directly
+# (its decks and its own test deck); they skip when IMC_REFERENCE is unset.
+REFERENCE = os.environ.get("IMC_REFERENCE", "")
+
+
+def reference_file(rel):
+    """Path of a file of the reference checkout, or None if it is absent."""
+    if not REFERENCE:
+        return None
+    p = os.path.join(REFERENCE, rel)
+    return p if os.path.exists(p) else None
 
 
 def pytest_configure(config):

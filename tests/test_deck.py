@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import DECKS, REFERENCE, deck_path, load_deck
+from conftest import DECKS, REFERENCE, deck_path, load_deck, reference_file
 
 import mpimc
 from mpimc import Input, Mesh
@@ -128,7 +128,7 @@ def test_build_deck_layout():
     assert C.sizeof(ImcDeck) == 6 * 4 + 10 * 8 + 16 + 24 + 8 + 8 + 8 + 16 + 8 + 8 + 8 + 8 + 8 + 40 + 16
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "src/inputs")), reason="reference checkout not present")
+@pytest.mark.skipif(reference_file("src/inputs") is None, reason="IMC_REFERENCE unset or without src/inputs")
 @pytest.mark.parametrize("name", ["SuOlson", "MarshakWave", "InfiniteMedium", "1DNonUniform", "2DNonUniform",
                                   "CrookedPipe"])
 def test_reference_decks_parse_and_mesh(name):
@@ -138,7 +138,7 @@ def test_reference_decks_parse_and_mesh(name):
     assert d.nx > 0 and d.n_scales >= 1
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(REFERENCE, "test/test_input.txt")),
+@pytest.mark.skipif(reference_file("test/test_input.txt") is None,
                     reason="reference checkout not present")
 def test_reference_test_deck():
     """The reference suite's own deck: readInputs gives a non-empty Dict with

@@ -12,7 +12,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import REFERENCE, deck_path, load_deck
+from conftest import REFERENCE, deck_path, load_deck, reference_file
 
 import oracle
 
@@ -168,7 +168,7 @@ def test_particle_budget_at_nmax():
 
 
 # --- (e) benchmark curve of the reference's Su-Olson deck
-@pytest.mark.skipif(not os.path.exists(os.path.join(REFERENCE, "src/inputs/SuOlson.txt")),
+@pytest.mark.skipif(reference_file("src/inputs/SuOlson.txt") is None,
                     reason="reference checkout not present")
 def test_suolson_benchmark_shape():
     """The radiation energy density at t = 10 follows the deck's XBENCH/YBENCH
