@@ -295,16 +295,21 @@ typedef struct ImcDeviceParticles {
 /* No counterpart in the reference.  Stable removal of the particles whose
  * alive byte is 0 -- the compaction imc_clean performs -- from caller-owned
  * device arrays `src` into caller-owned `dst`, for callers that cannot call
- * cudaMalloc: work enqueued during a CUDA stream capture, hosts whose device
- * memory belongs to their own pool allocator, loops that cannot take the
- * device-wide synchronisation of an allocation.  It allocates nothing: its
- * scratch is a fixed 72 KiB __device__ array that every GPU loading the
- * library holds until exit, which limits n to 16,777,216 particles (larger n
- * returns IMC_ERR_INVALID_ARG).  The first call on a device looks the array's
- * address up with that device current; make it before any stream capture.
- * All calls share the array, so calls that overlap on the GPU race.  Work is
- * ordered on `stream` (a cudaStream_t; NULL = the default stream); the call
- * returns once *n_out, the number of survivors, is known.
+ * cudaMalloc: hosts whose device memory belongs to their own pool allocator
+ * (which must account for every byte on the device), and loops that cannot
+ * take the device-wide synchronisation of an allocation.  It allocates
+ * nothing: its scratch is a fixed 72 KiB __device__ array that every GPU
+ * loading the library holds until exit, which limits n to 16,777,216
+ * particles (larger n returns IMC_ERR_INVALID_ARG).  The first call on a
+ * device looks the array's address up with that device current.  All calls
+ * share the array, so calls that overlap on the GPU race.
+ * Requirements, checked before any device work (IMC_ERR_INVALID_ARG):
+ * t, x, ux, E, E0, cs, alive non-NULL in both src and dst (2D: also y, uy);
+ * each array aligned to its element size, alive to 16 bytes; no dst array
+ * sharing memory with a src array over n elements (no in-place compaction).
+ * dst arrays hold at least n elements.  Work is ordered on `stream` (a
+ * cudaStream_t; NULL = the default stream); the call returns once *n_out,
+ * the number of survivors, is known.
  * Returns IMC_OK, IMC_ERR_INVALID_ARG, IMC_ERR_NO_DEVICE or IMC_ERR_CUDA. */
 int imc_clean_noalloc(int precision, int geometry, const ImcDeviceParticles *src, ImcDeviceParticles *dst,
                       int64_t n, int64_t *n_out, void *stream);
