@@ -3,16 +3,16 @@
 The reference's own tests hold no numeric golden vectors, so the oracle is
 checked against (a) published known-answer vectors of its generator, (b)
 closed-form results of the reference formulas, (c) the structural checks of
-the reference test suite, (d) conservation and equilibrium identities and
-(e) the benchmark curve carried in the reference's Su-Olson deck, read from
-the reference checkout when it is present.
+the reference test suite, (d) conservation and equilibrium identities.  The
+pin to the reference's own numbers -- the benchmark curves of its Su-Olson
+and Marshak-wave decks -- is tests/test_benchmark_curves.py.
 """
 import os
 
 import numpy as np
 import pytest
 
-from conftest import REFERENCE, deck_path, load_deck, reference_file
+from conftest import deck_path, load_deck
 
 import oracle
 
@@ -165,31 +165,3 @@ def test_particle_budget_at_nmax():
     budget = max(2.0, 6000 - nc - 1 - 1)
     # counts round per slot and each cell gets at least CELLMIN=2
     assert born <= budget + 2 * 10 + 2 * 10 + 2 and n1 > 0
-
-
-# --- (e) benchmark curve of the reference's Su-Olson deck
-@pytest.mark.skipif(reference_file("src/inputs/SuOlson.txt") is None,
-                    reason="reference checkout not present")
-def test_suolson_benchmark_shape():
-    """The radiation energy density at t = 10 follows the deck's XBENCH/YBENCH
-    curve.  Run at FP64 with the deck's physics but a coarser mesh and fewer
-    particles to keep the CPU time small; compare within MC noise."""
-    import mpimc
-    inputs = mpimc.Input.readInputs(os.path.join(REFERENCE, "src/inputs/SuOlson.txt"))
-    xb = np.array([float(v) for v in inputs["XBENCH"]])
-    yb = np.array([float(v) for v in inputs["YBENCH"]])
-    inputs["PRECISION"] = np.float64
-    inputs["DX"] = "0.05"
-    inputs["DT"] = "0.02"
-    inputs["ENDTIME"] = "1.0"
-    inputs["NINPUT"] = "3000"
-    inputs["ENERGYSCALES"] = ["1.0"]
-    mesh = mpimc.Mesh.mesh_generation(inputs)
-    o = oracle.Oracle(inputs, mesh)
-    o.run()
-    x = np.asarray(mesh.centers)
-    rad = o.field("radenergydens")
-    # the curve is quoted at t = 10; at t = 1 the wave has not reached x > 2
-    assert rad[x > 3.0].max() < 0.05 * rad.max()
-    assert np.all(np.isfinite(rad)) and rad.max() > 0
-    assert len(xb) == len(yb) > 5
