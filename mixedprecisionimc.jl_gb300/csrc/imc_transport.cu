@@ -84,10 +84,15 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     unsigned flags = 0;
     T emax = (T)0;
     // Lane state of the history in flight (cs: as stored in the list; the
-    // current cell and scale are cell, k).
+    // current cell and scale are cell, k).  Deposits go to the compensated
+    // pair (acc_s, acc_c) of the current cell acc_cell; the pair of the cell
+    // the history left last waits in (prv_s, prv_c, prv_cell) and is flushed
+    // only when a third cell is entered, so a history that visits at most
+    // two cells flushes both pairs at its end, with the warp converged.
     long long i = 0;
-    int cs = 0, cell = 0, k = 0, acc_cell = 0;
+    int cs = 0, cell = 0, k = 0, acc_cell = 0, prv_cell = -1;
     T t = (T)0, x = (T)0, mu = (T)0, E = (T)0, E0 = (T)0, minenergy = (T)0, acc_s = (T)0, acc_c = (T)0, rmu = (T)0;
+    T prv_s = (T)0, prv_c = (T)0;
     long long seg = 0;
     Stream rs;
     auto start = [&](int cs_now) {
@@ -98,6 +103,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         acc_s = (T)0;
         acc_c = (T)0;
         acc_cell = cell;
+        prv_cell = -1;
         seg = 0;
         rmu = (T)1 / mu;  // FP32: the face distance as a product (reset at each new direction)
     };
@@ -125,17 +131,25 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         }
         return true;
     };
-    // one pass of the reference's while loop; 0 = go on, 1 = killed or
-    // escaped, 2 = census, 3 = set aside for a query (kPause)
+    // the history is in `cell`: on a cell change the current pair moves to
+    // the waiting slot, whose earlier pair (a third cell) is flushed now
+    auto enter_cell = [&]() {
+        if (cell != acc_cell) {
+            if (prv_cell >= 0) flush_pair<T, SMT>(dep_acc, k * nc + prv_cell, prv_s, prv_c, b_dep, flags);
+            prv_cell = acc_cell; prv_s = acc_s; prv_c = acc_c;
+            acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
+        }
+    };
+    // one pass of the reference's while loop; 0 = go on, 1 = killed, 2 =
+    // census, 3 = set aside for a query (kPause), 4 = escaped through a
+    // vacuum face.  The census write and the escape tally are left to
+    // finish(), which the warp runs converged once per history.
     auto segment = [&]() -> int {
         if (gating && (float)(x < tab[cell].dxs - x ? x : tab[cell].dxs - x) * (float)tab[cell].seff >= gate[cell]) {
             Query q;
             const int kind = surr_decide<T>(tab[cell], x, mu, t, E, minenergy, c, ds, endsteptime, q);
             if (kind == kCertainKill) {
-                if (cell != acc_cell) {
-                    flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
-                    acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
-                }
+                enter_cell();
                 nadd(acc_s, acc_c, M::all_in(E, tab[cell]));
                 ++seg;
                 ++calls;
@@ -162,10 +176,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
             } else {
                 T dep;
                 const T newenergy = M::attenuate(E, ce, dist, &dep);
-                if (cell != acc_cell) {
-                    flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
-                    acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
-                }
+                enter_cell();
                 if (newenergy <= minenergy) {
                     nadd(acc_s, acc_c, M::all_in(E, ce));
                     end = 1;
@@ -182,8 +193,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
                                     mu = -mu;
                                     rmu = -rmu;
                                 } else {
-                                    flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
-                                    end = 1;
+                                    end = 4;
                                 }
                             }
                             if (!end) {
@@ -197,8 +207,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
                                     mu = -mu;
                                     rmu = -rmu;
                                 } else {
-                                    flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
-                                    end = 1;
+                                    end = 4;
                                 }
                             } else {
                                 cell -= 1;
@@ -214,40 +223,44 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
                         if (mu == (T)0) mu = (T)1;
                         rmu = (T)1 / mu;
                     }
-                    if (!end && dist == dist_cen) {
-                        // census: t = 0, write the state back (src/imc_transport.jl:185-193)
-                        T Est = E;
-                        if (St::half) {
-                            st_v(pb.t + i, 0.0f);
-                            st_v(pb.x + i, (float)x / (float)tab[cell].dxs);
-                            st_v(pb.ux + i, (float)mu);
-                            __half ef = __float2half_rn((float)E / (float)E0);
-                            pb.E[i] = ef;
-                            Est = __half2float(ef) * (float)E0;
-                        } else {
-                            pb.t[i] = (typename St::S)0;
-                            pb.x[i] = (typename St::S)x;
-                            pb.ux[i] = (typename St::S)mu;
-                            pb.E[i] = (typename St::S)E;
-                        }
-                        if (cell != (cs & 0xFFFFFF)) pb.cs[i] = cell | (k << 24);
-                        flush_one<T, RAD_SMT>(rad_acc, k * nc + cell, Est, b_rad, flags);
-                        emax = Est > emax ? Est : emax;
-                        end = 2;
-                    }
+                    // census: t = 0 and the state written back by finish()
+                    // (src/imc_transport.jl:185-193)
+                    if (!end && dist == dist_cen) end = 2;
                 }
             }
         }
         return end;
     };
     auto finish = [&](int end) {
+        if (prv_cell >= 0) flush_pair<T, SMT>(dep_acc, k * nc + prv_cell, prv_s, prv_c, b_dep, flags);
         flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
-        if (end == 3) {
+        if (end == 2) {
+            // census: t = 0, write the state back (src/imc_transport.jl:185-193)
+            T Est = E;
+            if (St::half) {
+                st_v(pb.t + i, 0.0f);
+                st_v(pb.x + i, (float)x / (float)tab[cell].dxs);
+                st_v(pb.ux + i, (float)mu);
+                __half ef = __float2half_rn((float)E / (float)E0);
+                pb.E[i] = ef;
+                Est = __half2float(ef) * (float)E0;
+            } else {
+                pb.t[i] = (typename St::S)0;
+                pb.x[i] = (typename St::S)x;
+                pb.ux[i] = (typename St::S)mu;
+                pb.E[i] = (typename St::S)E;
+            }
+            if (cell != (cs & 0xFFFFFF)) pb.cs[i] = cell | (k << 24);
+            flush_one<T, RAD_SMT>(rad_acc, k * nc + cell, Est, b_rad, flags);
+            emax = Est > emax ? Est : emax;
+        } else if (end == 3) {
             // set aside with its state for the query pass (its deposits flushed)
             const unsigned long long j = atomicAdd(ask_count, 1ull);
             w.ask.x[j] = (float)x; w.ask.mu[j] = (float)mu; w.ask.t[j] = (float)t; w.ask.E[j] = (float)E;
             w.ask.E0[j] = (float)E0; w.ask.cs[j] = cell | (k << 24); w.ask.cs_list[j] = cs; w.ask.idx[j] = i;
-        } else if (end == 1) {
+        } else {
+            // killed, or escaped with E through a vacuum face
+            if (end == 4) flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
             pb.alive[i] = 0;
             ++killed;
         }

@@ -104,6 +104,39 @@ def test_transport_parity_fp32(gpu_lib):
     np.testing.assert_allclose(dg, do, rtol=1e-3, atol=1e-6 * np.abs(do).max())
 
 
+def test_transport_parity_fp32_2d(gpu_lib):
+    """Transport.MC2D (src/imc_transport.jl:483-732) with FP32 state, in the
+    FP32 formulation the kernel and the oracle share: direction cosines,
+    -log(v)/seff collision distances with the hardware logarithm, one expm1
+    for attenuation and deposit, reciprocal cell areas.  The kernel re-emits
+    with the hardware sine and cosine (the oracle with libm's, ~1 ulp apart),
+    so histories that collide carry 1e-7-level direction differences:
+    positions, times and weights agree to 1e-4 for >= 99% of histories."""
+    g, o = _pair("tiny_2d", gpu_lib, PRECISION=np.float32)
+    for e in (g, o):
+        e.update()
+        e.sourcing()
+    _cmp_particles(g, o, rtol=1e-6, keys=("t", "x", "y", "E", "E0"))
+    for e in (g, o):
+        e.transport()
+    _cmp_particles(g, o, rtol=1e-4, frac_ok=0.99, keys=("t", "x", "y", "E"))
+    dg, do = g.field("energydep"), o.field("energydep")
+    np.testing.assert_allclose(dg, do, rtol=1e-3, atol=1e-6 * np.abs(do).max())
+
+
+def test_step_parity_fp32_2d(gpu_lib):
+    """Three FP32 2D steps track the oracle's FP32 steps (fields to 1e-3)."""
+    g, o = _pair("tiny_2d", gpu_lib, PRECISION=np.float32)
+    for _ in range(3):
+        sg, _ = g.step()
+        so, _ = o.step()
+        assert sg["n_sourced"] == so["n_sourced"]
+        assert abs(sg["n_census_out"] - so["n_census_out"]) <= max(3, 1e-3 * so["n_census_out"])
+    for f in ("temp", "radenergydens", "matenergydens"):
+        a, b = g.field(f), o.field(f)
+        np.testing.assert_allclose(a, b, rtol=1e-3, atol=1e-6 * np.abs(b).max(), err_msg=f)
+
+
 def test_energy_conservation_fp64(gpu_lib):
     """src/imc_energycheck.jl:34 balance: <= 1e-10 relative in FP64 (1D, no
     2D source quirk)."""

@@ -7,7 +7,6 @@ the reference test suite, (d) conservation and equilibrium identities.  The
 pin to the reference's own numbers -- the benchmark curves of its Su-Olson
 and Marshak-wave decks -- is tests/test_benchmark_curves.py.
 """
-import os
 
 import numpy as np
 import pytest
