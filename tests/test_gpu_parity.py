@@ -217,3 +217,42 @@ def test_step_parity_fp64_2d_large_mesh(gpu_lib, ysize):
     for f in ("temp", "radenergydens", "matenergydens"):
         a, b = g.field(f), o.field(f)
         np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-9 * np.abs(b).max(), err_msg=f)
+
+
+# FP32 selection needs products beyond binary32's range to fall back
+_MULTISCALE = {
+    "fp16": {"PRECISION": np.float16},
+    "fp32": {"PRECISION": np.float32, "ENERGYSCALES": ["1e38", "1000.0", "1.0"],
+             "RADSOURCE_VALS": ["1e6", "1e4", "100.0", "0.01", "0.0"]},
+}
+
+
+@pytest.mark.parametrize("prec", ["fp16", "fp32"])
+def test_multiscale_sorter_fallback_parity(gpu_lib, prec):
+    """Utilities.sorter's retry with the next energy scale
+    (src/imc_utilities.jl:23-54) on the device, in the deck precision: the
+    multi-scale slab's slots overflow binary16 (binary32) at the first scales,
+    so its births carry several scale indices.  Sourcing equals the oracle
+    particle for particle (scale index included); three steps track the
+    oracle's fields and balance."""
+    g, o = _pair("multiscale_1d", gpu_lib, **_MULTISCALE[prec])
+    for e in (g, o):
+        e.update()
+        e.sourcing()
+    assert g.num_particles() == o.num_particles() > 0
+    pg, po = g.particles(), o.particles()
+    assert len(np.unique(po["scale"])) >= 2, "the deck no longer exercises the fallback"
+    np.testing.assert_array_equal(pg["scale"], po["scale"])
+    np.testing.assert_allclose(g.field("emittedenergy"), o.field("emittedenergy"), rtol=1e-14)
+    _cmp_particles(g, o, rtol=1e-6, keys=("t", "x", "mu", "E", "E0"))
+    g, o = _pair("multiscale_1d", gpu_lib, **_MULTISCALE[prec])
+    for _ in range(3):
+        sg, _ = g.step()
+        so, _ = o.step()
+        assert sg["n_sourced"] == so["n_sourced"]
+        assert sg["error_flags"] == 0
+        np.testing.assert_allclose(sg["total_energy"], so["total_energy"], rtol=1e-13)
+        assert abs(sg["energy_error"] - so["energy_error"]) < 1e-4
+    for f in ("temp", "radenergydens", "matenergydens"):
+        a, b = g.field(f), o.field(f)
+        np.testing.assert_allclose(a, b, rtol=2e-3, atol=1e-6 * np.abs(b).max(), err_msg=f)
