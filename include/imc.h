@@ -307,7 +307,8 @@ typedef struct ImcDeviceParticles {
  * t, x, ux, E, E0, cs, alive non-NULL in both src and dst (2D: also y, uy);
  * each array aligned to its element size, alive to 16 bytes; no dst array
  * sharing memory with a src array over n elements (no in-place compaction).
- * dst arrays hold at least n elements.  Work is ordered on `stream` (a
+ * dst arrays hold at least n elements; with n = 0 no array is read (NULL
+ * is accepted) and *n_out = 0.  Work is ordered on `stream` (a
  * cudaStream_t; NULL = the default stream); the call returns once *n_out,
  * the number of survivors, is known.
  * Returns IMC_OK, IMC_ERR_INVALID_ARG, IMC_ERR_NO_DEVICE or IMC_ERR_CUDA. */

@@ -96,6 +96,11 @@ extern "C" int imc_clean_noalloc(int precision, int geometry, const ImcDevicePar
     const long long ntiles = (n + kCompactTile - 1) / kCompactTile;
     if (ntiles > kNoAllocMaxTiles)
         return IMC_ERR_INVALID_ARG;
+    // an empty list reads and writes no array (which may then be NULL)
+    if (n == 0) {
+        *n_out = 0;
+        return IMC_OK;
+    }
     Field fs[9], fd[9];
     int ns = 0, nd = 0;
     if (!fields_of(src, precision, geometry, fs, &ns) || !fields_of(dst, precision, geometry, fd, &nd))
@@ -122,7 +127,6 @@ extern "C" int imc_clean_noalloc(int precision, int geometry, const ImcDevicePar
     }
     cudaStream_t st = (cudaStream_t)stream;
     *n_out = 0;
-    if (n == 0) return IMC_OK;
     Scalars *sc = (Scalars *)base;
     long long *tile_cnt = (long long *)(base + kNoAllocScalarsBytes);
     long long *tile_off = tile_cnt + (kNoAllocMaxTiles + 1);
