@@ -15,7 +15,8 @@ Tolerances, stated once:
   where the curve is above 0.75 (behind the front), |mean - bench| <=
   3 sigma_mean + 2 % of bench; the front (where T first falls below 0.3)
   within 0.0025 (5 cells) of the curve's; ahead of the front (curve below
-  0.02), the mean temperature within 5 % of the curve's mean there.
+  0.02, from 5 cells past the curve's front on), the mean temperature within
+  5 % of the curve's mean there.
 """
 import os
 
@@ -63,7 +64,7 @@ def marshak_violations(centers, mean, sem):
     fb, fm = front(xb, yb), front(centers, mean)
     if abs(fb - fm) > 0.0025:
         out.append("front bench %.5f got %.5f" % (fb, fm))
-    cold = yb < 0.02
+    cold = (yb < 0.02) & (xb > fb + 0.0025)
     if abs(m[cold].mean() / yb[cold].mean() - 1.0) > 0.05:
         out.append("cold mean bench %.5f got %.5f" % (yb[cold].mean(), m[cold].mean()))
     return out
