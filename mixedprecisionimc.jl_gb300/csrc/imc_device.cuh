@@ -337,6 +337,24 @@ IMC_HD bool fix_split(float v, int b, Limbs &o) {
     o.l0 = l0; o.l1 = l1; o.l2 = l2;
     return true;
 }
+// The same placement for a positive normal FP32 value, as two 32-bit words:
+// bits [32j, 32j + 32) of the fixed-point value get lo, the next word hi (0
+// when j == 2).  False where fix_split would round (below the resolution),
+// fail (above the range, not finite) or negate; the shared-memory tally
+// flush takes this path and leaves the rest to fix_split.
+IMC_HD bool f32_words(float v, int b, int &j, uint32_t &lo, uint32_t &hi) {
+    const uint32_t bits = f2u(v);
+    const int ex = (int)(bits >> 23);  // the sign bit makes it >= 256
+    if (ex == 0 || ex >= 255) return false;
+    const int sh = ex - 150 - b;  // exponent of the mantissa's lowest bit, relative to b
+    if (sh < 0 || sh > 94 - 24) return false;
+    const uint32_t man = (bits & 0x7FFFFFu) | 0x800000u;
+    j = sh >> 5;
+    const int off = sh & 31;
+    lo = man << off;
+    hi = off ? man >> (32 - off) : 0u;
+    return true;
+}
 IMC_HD bool fix_split(double v, int b, Limbs &o) {
     uint64_t bits = d2u(v);
     bool neg = (bits >> 63) != 0;

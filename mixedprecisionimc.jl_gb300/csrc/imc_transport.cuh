@@ -49,6 +49,27 @@ __device__ __forceinline__ void add_word_smem(unsigned *w, int *cy, long long l)
     if (c) atomicAdd_block(cy, c);
 }
 
+// A positive FP32 value into a shared slot, without the signed three-limb
+// split: its 24-bit mantissa occupies at most two adjacent 32-bit words of the
+// 96-bit fixed-point value (f32_words), so at most two word adds (slot word
+// 2 - j holds bits 32j..32j+31, as in add_limbs).  The same integers as
+// fix_split + add_limbs<true>, so the same sums.  False (nothing added) for a
+// value the general path must handle (see f32_words).
+__device__ __forceinline__ void add_word_u(unsigned *w, int *cy, unsigned u) {
+    const unsigned old = atomicAdd_block(w, u);
+    if (old + u < old) atomicAdd_block(cy, 1);
+}
+__device__ __forceinline__ bool add_f32_smem(long long *slot, float v, int b) {
+    int j;
+    uint32_t lo, hi;
+    if (!f32_words(v, b, j, lo, hi)) return false;
+    unsigned *w = reinterpret_cast<unsigned *>(slot);
+    int *cy = reinterpret_cast<int *>(slot) + 3;
+    if (lo) add_word_u(w + 2 - j, cy + 2 - j, lo);
+    if (hi) add_word_u(w + 1 - j, cy + 1 - j, hi);
+    return true;
+}
+
 template <bool SMT> __device__ __forceinline__ void add_limbs(long long *a, const Limbs &L) {
     if (SMT) {
         // the pointer is known to address shared memory
@@ -121,6 +142,8 @@ template <class T, bool SMT>
 __device__ __forceinline__ void flush_pair(long long *acc, int slot, T s, T c, int b, unsigned &flags) {
     const T v = s + c;
     if (v == (T)0) return;
+    if constexpr (SMT && sizeof(T) == 4)
+        if (add_f32_smem(acc + 3 * (size_t)slot, v, b)) return;
     Limbs A;
     if (!fix_split(v, b, A)) {
         flags |= (v != v) ? 1u /*NAN*/ : (1u << 5) /*FIXPOINT_RANGE*/;
@@ -132,6 +155,8 @@ __device__ __forceinline__ void flush_pair(long long *acc, int slot, T s, T c, i
 template <class T, bool SMT>
 __device__ __forceinline__ void flush_one(long long *acc, int slot, T v, int b, unsigned &flags) {
     if (v == (T)0) return;
+    if constexpr (SMT && sizeof(T) == 4)
+        if (add_f32_smem(acc + 3 * (size_t)slot, v, b)) return;
     Limbs A;
     if (!fix_split(v, b, A)) {
         flags |= (v != v) ? 1u : (1u << 5);

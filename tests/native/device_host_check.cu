@@ -6,6 +6,10 @@
 //   F b v1 v2 ... (until '.')    -> exact fixed-point total of the values, as
 //                                   signed limb sums "a0 a1 a2" and the double
 //   R prec n v1..vn K s1..sK     -> sorter<prec> product (hex) and scale index
+//   W b v1 v2 ... (until '.')    -> per FP32 value: "1 l0 l1 l2" from f32_words
+//                                   (words as the signed limbs of fix_split),
+//                                   "0" where f32_words declines, and
+//                                   fix_split's "ok l0 l1 l2" after it
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -45,6 +49,20 @@ int main() {
                 acc[0] += L.l0; acc[1] += L.l1; acc[2] += L.l2;
             }
             printf("%d %lld %lld %lld %.17g\n", ok ? 1 : 0, acc[0], acc[1], acc[2], fix_value(acc, b));
+        } else if (cmd == "W") {
+            int b; in >> b;
+            std::string tok;
+            while (in >> tok && tok != ".") {
+                const float v = strtof(tok.c_str(), nullptr);
+                int j; uint32_t lo, hi;
+                long long w[3] = {0, 0, 0};  // bits 0-31, 32-63, 64-95
+                const bool f = f32_words(v, b, j, lo, hi);
+                if (f) { w[j] = lo; if (j < 2) w[j + 1] = hi; else if (hi) w[0] = -1; }
+                Limbs L;
+                const bool r = fix_split(v, b, L);
+                printf("%d %lld %lld %lld %d %lld %lld %lld\n", f ? 1 : 0, w[2], w[1], w[0], r ? 1 : 0,
+                       r ? L.l0 : 0, r ? L.l1 : 0, r ? L.l2 : 0);
+            }
         } else if (cmd == "R") {
             int prec, n, K;
             in >> prec >> n;

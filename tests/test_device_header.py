@@ -119,3 +119,31 @@ def test_sorter_special_values_match_oracle(tool, prec):
         assert int(j) == jo, (v, s)
         pg = float.fromhex(p_hex)
         assert pg == p and np.signbit(pg) == np.signbit(p), (v, s, pg, p)
+
+
+def test_f32_two_word_placement_equals_fix_split(tool):
+    """The shared-memory flush's FP32 path (f32_words: a positive normal value
+    as at most two adjacent 32-bit words) places exactly the bits fix_split
+    does wherever it applies, and declines zero, subnormal, negative,
+    non-finite, below-resolution and out-of-range values (left to fix_split)."""
+    rng = np.random.default_rng(3)
+    for b in (-93, -60, -30, 0, 17):
+        vals = list(np.float32(rng.uniform(0.5, 1.0, 200) * 2.0 ** rng.integers(-80, 40, 200)))
+        vals += [np.float32(2.0 ** e) for e in range(-149, 128, 7)]
+        vals += [0.0, -1.5, np.float32(1e-45), float("inf"), float("nan"), np.float32(3.4e38)]
+        toks = ["%r" % float(v) for v in vals]
+        out = tool(["W %d %s ." % (b, " ".join(toks))])
+        assert len(out) == len(vals)
+        took = 0
+        for v, line in zip(vals, out):
+            f, w2, w1, w0, ok, l0, l1, l2 = map(int, line.split())
+            if f:
+                took += 1
+                assert ok == 1 and (w2, w1, w0) == (l0, l1, l2), (b, v, line)
+                assert v > 0 and np.isfinite(v)
+            elif ok == 1 and v > 0 and np.float32(v) >= np.float32(2.0 ** -126):
+                # declined although fix_split places it: only below the
+                # resolution (fix_split rounds there)
+                e = int(np.floor(np.log2(v)))
+                assert e - 23 - b < 0, (b, v, line)
+        assert took > 20
