@@ -1,5 +1,6 @@
 """FP64 oracle ensembles of the slab, heat-wave and channel decks at reduced
-particle counts: tests/golden/oracle_fp64_ensembles.npz.
+particle counts, and of the heated thick slab at full size:
+tests/golden/oracle_fp64_ensembles.npz.
 
 The CPU oracle (the restatement of the reference path) runs each deck with its
 mesh, physics and clock unchanged -- the 2000-cell slab to t = 3 (602 steps),
@@ -10,7 +11,12 @@ NINPUT / NMAX scaled down (REDUCED below), 32 seeds each, FP64 particle state.
 The GPU tests (tests/test_gpu_oracle_ensembles.py) run the same reduced decks
 in every state precision and compare their ensemble means with these per cell.
 
-Run from the repository root:  python tests/golden/make_oracle_ensembles.py [c2 c3 c4]
+The heated thick slab (tests/golden/decks/thick_heated.txt: 30 cells of 40
+mean free paths, a source in every cell, vacuum on the right) runs as
+written; its mean is the error reference of the learned surrogate's
+comparison in bench.py, where every arm reaches an error below 1 %.
+
+Run from the repository root:  python tests/golden/make_oracle_ensembles.py [c2 c3 c4 thick]
 """
 import multiprocessing as mp
 import os
@@ -27,6 +33,7 @@ REDUCED = {
     "c2": ("c2_slab_fine", {"NINPUT": "20000", "NMAX": "200000"}),
     "c3": ("c3_heatwave", {"NINPUT": "20000", "NMAX": "200000"}),
     "c4": ("c4_channel2d", {"NINPUT": "10000", "NMAX": "50000"}),
+    "thick": ("thick_heated", {}),
 }
 SEEDS = [500000 + i for i in range(32)]
 
@@ -59,7 +66,7 @@ def one(args):
 
 
 def main():
-    names = [a for a in sys.argv[1:] if a in REDUCED] or list(REDUCED)
+    names = [a for a in sys.argv[1:] if a in REDUCED] or [n for n in REDUCED if n != "thick"]
     out = dict(np.load(OUT)) if os.path.exists(OUT) else {}
     with mp.get_context("spawn").Pool(min(8, os.cpu_count() or 1)) as pool:
         for name in names:
