@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "imc.h"  // include/imc.h (on the -I path)
+#include "imc_device.cuh"
 #include "imc_internal.h"
 #include "imc_surrogate.cuh"
 
@@ -38,7 +39,11 @@ struct Stage { enum { Fresh = 0, Updated, Sourced, Transported, Cleaned, Tallied
 }  // namespace
 
 struct ImcHandle {
+    // the deck's scalars; the arrays read after imc_create (cell widths,
+    // energy scales) point into host_dx / host_dy / host_scales, copies the
+    // handle owns: the caller's arrays are read during imc_create only
     ImcDeck deck;
+    std::vector<double> host_dx, host_dy, host_scales;
     int device = 0, sm_count = 0;
     cudaStream_t stream = nullptr;
     int prec = 1, geometry = 1, nx = 1, ny = 1, nc = 1, K = 1, nslots = 0;
@@ -486,6 +491,12 @@ int imc_create(const ImcDeck *d, ImcHandle **out) {
     if (rc) return fail(nullptr, rc, why);
     ImcHandle *h = new ImcHandle();
     h->deck = *d;
+    h->host_dx.assign(d->dx, d->dx + d->nx);
+    if (d->geometry == IMC_GEOM_2D) h->host_dy.assign(d->dy, d->dy + d->ny);
+    h->host_scales.assign(d->energyscales, d->energyscales + d->n_scales);
+    h->deck.dx = h->host_dx.data();
+    h->deck.dy = d->geometry == IMC_GEOM_2D ? h->host_dy.data() : nullptr;
+    h->deck.energyscales = h->host_scales.data();
     auto bail = [&](int code) {
         g_create_err = h->err; g_create_code = code;
         imc_destroy(h);
@@ -565,6 +576,7 @@ int imc_create(const ImcDeck *d, ImcHandle **out) {
     if ((rc = tile_alloc(h))) return bail(rc);
     // scalars
     Scalars sc{};
+    sc.emax_census_exp = kNoExp;
     h->t = 0.0;
     h->dt = d->timestepping == IMC_TS_RAMP ? d->dt0 : d->dt;
     sc.t = h->t; sc.dt = h->dt;
@@ -953,7 +965,7 @@ struct StateHeader {
     int64_t step, finished, tot_segments, tot_histories, tot_calls;
     int64_t scalars_bytes;  // the device scalars' layout must match too
 };
-constexpr int32_t kStateVersion = 2;
+constexpr int32_t kStateVersion = 3;  // 3: census maximum kept as an exponent per true energy
 
 struct Piece {
     void *dev;
@@ -1115,7 +1127,7 @@ int imc_set_particles(ImcHandle *h, const ImcParticles *p) {
     std::vector<unsigned char> t(se * n), x(se * n), y(se * n), ux(se * n), uy(se * n), E(se * n), E0(e0s * n);
     std::vector<int32_t> cs(n);
     std::vector<uint8_t> alive(n);
-    double emax = 0.0;
+    int emax_e = kNoExp;  // census maximum as the ilogb of its true energy
     auto wr = [&](std::vector<unsigned char> &v, long long i, double val) {
         if (prec == 0) ((double *)v.data())[i] = val;
         else if (prec == 1) ((float *)v.data())[i] = (float)val;
@@ -1126,6 +1138,7 @@ int imc_set_particles(ImcHandle *h, const ImcParticles *p) {
         if (cell < 0 || cell >= h->nc) return fail(h, IMC_ERR_INVALID_ARG, "particle cell out of range");
         const int k = p->scale ? p->scale[i] : 0;
         if (k < 0 || k >= h->K) return fail(h, IMC_ERR_INVALID_ARG, "particle scale index out of range");
+        const int se = scale_exp(h->deck.energyscales[k]);
         const int ix = h->geometry == 1 ? cell : cell % h->nx;
         const int iy = h->geometry == 1 ? 0 : cell / h->nx;
         const double vt = p->t ? p->t[i] : 0.0, vx = p->x ? p->x[i] : 0.0, vy = p->y ? p->y[i] : 0.0;
@@ -1142,12 +1155,12 @@ int imc_set_particles(ImcHandle *h, const ImcParticles *p) {
             ((float *)E0.data())[i] = (float)vE0;
             float ef = (float)vE / (float)vE0;
             wr(E, i, (double)ef);
-            if (alive[i]) emax = std::max(emax, (double)(__half2float(__float2half_rn(ef)) * (float)vE0));
+            if (alive[i]) emax_e = std::max(emax_e, exp_bound(__half2float(__float2half_rn(ef)) * (float)vE0) - se);
         } else {
             wr(t, i, vt); wr(x, i, vx); wr(y, i, vy); wr(E, i, vE);
             if (prec == 0) ((double *)E0.data())[i] = vE0;
             else ((float *)E0.data())[i] = (float)vE0;
-            if (alive[i]) emax = std::max(emax, prec == 0 ? vE : (double)(float)vE);
+            if (alive[i]) emax_e = std::max(emax_e, (prec == 0 ? exp_bound(vE) : exp_bound((float)vE)) - se);
         }
         wr(ux, i, dirx);
         wr(uy, i, diry);
@@ -1172,9 +1185,7 @@ int imc_set_particles(ImcHandle *h, const ImcParticles *p) {
     for (long long i = 0; i < n; ++i) live += alive[i];
     sc.n_census = live;
     sc.n_particles = n;
-    union { double d; unsigned long long u; } cv;
-    cv.d = emax;
-    sc.emax_census_bits = cv.u;
+    sc.emax_census_exp = emax_e;
     CK(h, hcopy(h, h->d_sc, &sc, sizeof(Scalars), cudaMemcpyHostToDevice));
     h->stage = Stage::Fresh;
     return IMC_OK;

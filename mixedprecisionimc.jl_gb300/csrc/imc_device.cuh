@@ -12,6 +12,7 @@
 //    addition is associative, so the tally does not depend on the order in
 //    which histories finish: GPU runs are bit-reproducible run to run.
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <cuda_fp16.h>
@@ -365,6 +366,37 @@ IMC_HD bool fix_split(double v, int b, Limbs &o) {
     if (ex == 0) e2 = 1 - 1023 - 52;
     else { man |= 0x10000000000000ull; e2 = ex - 1023 - 52; }
     return fix_place(man, e2 - b, neg, o);
+}
+
+// Energy scales and the tally exponents.  A particle of scale k carries
+// E = e_true * scale_k; each tally slot of scale k holds its values times
+// 2^-scale_exp(scale_k), i.e. within a factor two of true energies, so one
+// exponent per tally (set from the largest true energy) fits every scale --
+// scale lists that span more than the fixed point's 2^93 (the binary32
+// fallback of the sorter) lose nothing.  The tallies' exponent of scale k is
+// that base plus scale_exp(scale_k); exact powers of two throughout.
+IMC_HD int scale_exp(double s) {
+    const int e = (int)((d2u(s) >> 52) & 0x7FFu);
+    return e == 0 ? -1023 : e - 1023;  // ilogb of a normal scale
+}
+// an upper bound of ilogb(v) for v > 0: exact for normal v
+IMC_HD int exp_bound(float v) {
+    const int e = (int)((f2u(v) >> 23) & 0xFFu);
+    return e == 0 ? -127 : e - 127;
+}
+IMC_HD int exp_bound(double v) {
+    const int e = (int)((d2u(v) >> 52) & 0x7FFu);
+    return e == 0 ? -1023 : e - 1023;
+}
+// no census particle (emax_census_exp of an empty census)
+constexpr int kNoExp = -100000;
+// the largest double whose ilogb is e (every value of that exponent is <= it)
+IMC_HD double exp_top(int e) {
+#ifdef __CUDA_ARCH__
+    return ldexp(1.9999999999999998, e);
+#else
+    return std::ldexp(1.9999999999999998, e);
+#endif
 }
 
 // Exponent b with every |v| <= vmax mapping below 2^93 (one spare bit for a

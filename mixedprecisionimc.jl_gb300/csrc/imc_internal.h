@@ -30,8 +30,8 @@ struct Scalars {
     double t, dt;
     double totalenergy, totalenergydep, lostenergy, radenergyold, radenergy, energy_err;
     double lost_step;                  // escaped energy of this step
-    unsigned long long emax_census_bits;  // max census energy (bits of a non-negative double)
-    double emax;                       // max particle energy at transport start
+    int emax_census_exp;               // max over the census of ilogb(E) - scale_exp(scale_k) (kNoExp: none)
+    double emax;                       // max true particle energy at transport start (an upper bound)
     long long n_census;                // live particles in the list (the census after transport)
     long long n_census_in;             // census carried into this step
     long long n_particles;             // list length (live particles and holes left by kills)
@@ -46,7 +46,8 @@ struct Scalars {
     unsigned long long work_next;      // transport: next chunk of the list's tail to hand out
     unsigned long long qcount[2 * kSurrRounds + 1];  // surrogate transport: ask queue of round r at 2r, resume queue at 2r + 1
     unsigned int flags;
-    int b_dep, b_rad, b_lost;          // fixed-point exponents of this transport
+    int b_dep, b_rad, b_lost;          // fixed-point exponents of this transport in true energy;
+                                       // scale k's tallies use b + scale_exp(scale_k)
     unsigned int step;                 // step index (RNG key, stats slot)
     int finished;                      // t > t_end
     int cur;                           // particle buffer holding the list (0 or 1)

@@ -284,7 +284,8 @@ __global__ void __launch_bounds__(kCellThreads) k_source_counts(CellArgs ca, Sca
         const double nrg = n > 0 ? e[q] / (double)nd : 0.0;
         ca.slot_n[q] = n;
         ca.slot_nrg[q] = nrg;
-        if (n > 0) my = nrg;
+        // the largest birth energy in true units (see scale_exp)
+        if (n > 0) my = ldexp(nrg, -scale_exp(ca.scales[ca.slot_j[q]]));
     }
     for (int off = 16; off > 0; off >>= 1) {
         double o = __shfl_down_sync(0xFFFFFFFFu, my, off);
@@ -351,13 +352,14 @@ __global__ void __launch_bounds__(kPlanThreads) k_source_scan(CellArgs ca, Scala
             if (n_new < 0) n_new = 0;
             fl |= 1u << 3;
         }
-        const double emax = fmax(__longlong_as_double((long long)sc->emax_census_bits), s_emax);
+        const int ce = sc->emax_census_exp;
+        const double emax = fmax(ce == kNoExp ? 0.0 : exp_top(ce), s_emax);
         sc->n_census_in = n_census;
         sc->n_sourced = n_new;
         sc->birth_base = len;
         sc->n_particles = len + n_new;
         sc->emax = emax;
-        sc->emax_census_bits = 0ull;
+        sc->emax_census_exp = kNoExp;
         sc->segments = 0ull;
         sc->surrogate_calls = 0ull;
         sc->killed = 0ull;
@@ -729,11 +731,12 @@ __device__ __forceinline__ void finalize_cell(const CellArgs &ca, Scalars *sc, i
         double r = 0.0;
         for (int k = 0; k < K; ++k) {
             const size_t idx = (size_t)k * nc + i;
+            const int se = scale_exp(ca.scales[k]);
             long long *d = ca.dep_acc + 3 * idx;
-            ca.energydep[idx] = fix_value(d, b_dep);
+            ca.energydep[idx] = fix_value(d, b_dep + se);
             d[0] = d[1] = d[2] = 0;
             long long *g = ca.rad_acc + 3 * idx;
-            r += fix_value(g, b_rad) / (vol * ca.scales[k]);
+            r += fix_value(g, b_rad + se) / (vol * ca.scales[k]);
             g[0] = g[1] = g[2] = 0;
         }
         ca.radenergydens[i] = r;
@@ -742,7 +745,7 @@ __device__ __forceinline__ void finalize_cell(const CellArgs &ca, Scalars *sc, i
         double lost = 0.0;
         for (int k = 0; k < K; ++k) {
             long long *d = ca.lost_acc + 3 * k;
-            lost += fix_value(d, b_lost) / ca.scales[k];
+            lost += fix_value(d, b_lost + scale_exp(ca.scales[k])) / ca.scales[k];
             d[0] = d[1] = d[2] = 0;
         }
         sc->lost_step = lost;
@@ -906,9 +909,10 @@ void launch_energycheck_timestep(const CellArgs &ca, Scalars *sc, DevStats *stat
 // Transport of a list that was set directly (no sourcing this step): take the
 // fixed-point exponents from the census maximum.
 __global__ void k_prepare_transport(CellArgs ca, Scalars *sc) {
-    double emax = __longlong_as_double((long long)sc->emax_census_bits);
+    const int ce = sc->emax_census_exp;
+    const double emax = ce == kNoExp ? 0.0 : exp_top(ce);
     sc->emax = emax;
-    sc->emax_census_bits = 0ull;
+    sc->emax_census_exp = kNoExp;
     sc->segments = 0ull;
     sc->surrogate_calls = 0ull;
     sc->killed = 0ull;

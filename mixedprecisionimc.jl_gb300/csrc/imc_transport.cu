@@ -64,6 +64,8 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     const T endsteptime = (T)sc->dt;
     float *gate = reinterpret_cast<float *>(smem_raw + analog1d_smem(ca, sizeof(T), RAD_SMT, false));
     for (int i = threadIdx.x; i < N; i += blockDim.x) tab[i] = make_tab1<T>(ca.sa[i], ca.fleck[i], ca.ss[i], ca.dx[i], ds);
+    __shared__ int s_sexp[16];
+    load_scale_exps(ca, s_sexp);
     if (kPause) fill_gate<T>(ca, gate, ds, c, endsteptime);
     // the barrier after the table; with the gate, also whether any cell's
     // gate is open this step (each thread tests the entries it filled; every
@@ -82,7 +84,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     const uint32_t stage = kFromQueue ? kStageResume + (uint32_t)round : kStageTransport;
     unsigned long long segs = 0, calls = 0, killed = 0;
     unsigned flags = 0;
-    T emax = (T)0;
+    int emax_e = kNoExp;
     // Lane state of the history in flight (cs: as stored in the list; the
     // current cell and scale are cell, k).  Deposits go to the compensated
     // pair (acc_s, acc_c) of the current cell acc_cell; the pair of the cell
@@ -135,7 +137,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     // the waiting slot, whose earlier pair (a third cell) is flushed now
     auto enter_cell = [&]() {
         if (cell != acc_cell) {
-            if (prv_cell >= 0) flush_pair<T, SMT>(dep_acc, k * nc + prv_cell, prv_s, prv_c, b_dep, flags);
+            if (prv_cell >= 0) flush_pair<T, SMT>(dep_acc, k * nc + prv_cell, prv_s, prv_c, b_dep + s_sexp[k], flags);
             prv_cell = acc_cell; prv_s = acc_s; prv_c = acc_c;
             acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
         }
@@ -232,8 +234,9 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         return end;
     };
     auto finish = [&](int end) {
-        if (prv_cell >= 0) flush_pair<T, SMT>(dep_acc, k * nc + prv_cell, prv_s, prv_c, b_dep, flags);
-        flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+        const int se = s_sexp[k];
+        if (prv_cell >= 0) flush_pair<T, SMT>(dep_acc, k * nc + prv_cell, prv_s, prv_c, b_dep + se, flags);
+        flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep + se, flags);
         if (end == 2) {
             // census: t = 0, write the state back (src/imc_transport.jl:185-193)
             T Est = E;
@@ -251,8 +254,9 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
                 pb.E[i] = (typename St::S)E;
             }
             if (cell != (cs & 0xFFFFFF)) pb.cs[i] = cell | (k << 24);
-            flush_one<T, RAD_SMT>(rad_acc, k * nc + cell, Est, b_rad, flags);
-            emax = Est > emax ? Est : emax;
+            flush_one<T, RAD_SMT>(rad_acc, k * nc + cell, Est, b_rad + se, flags);
+            const int ee = exp_bound(Est) - se;
+            emax_e = ee > emax_e ? ee : emax_e;
         } else if (end == 3) {
             // set aside with its state for the query pass (its deposits flushed)
             const unsigned long long j = atomicAdd(ask_count, 1ull);
@@ -260,7 +264,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
             w.ask.E0[j] = (float)E0; w.ask.cs[j] = cell | (k << 24); w.ask.cs_list[j] = cs; w.ask.idx[j] = i;
         } else {
             // killed, or escaped with E through a vacuum face
-            if (end == 4) flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
+            if (end == 4) flush_one<T, false>(ca.lost_acc, k, E, b_lost + se, flags);
             pb.alive[i] = 0;
             ++killed;
         }
@@ -354,7 +358,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         for (int off = 16; off > 0; off >>= 1) calls += __shfl_down_sync(0xFFFFFFFFu, calls, off);
         if (lane == 0 && calls) atomicAdd(&sc->surrogate_calls, calls);
     }
-    finish_counters<T>(sc, segs, killed, flags, emax);
+    finish_counters(sc, segs, killed, flags, emax_e);
 }
 
 // TM, where the flushes go: kTallyGlobal, kTallyShared (deposition and
@@ -394,6 +398,8 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
     }
     for (int i = threadIdx.x; i < NX; i += blockDim.x) { fx[i].wT = (T)ca.dx[i]; fx[i].ws = fx[i].wT * ds; }
     for (int i = threadIdx.x; i < NY; i += blockDim.x) { fy[i].wT = (T)ca.dy[i]; fy[i].ws = fy[i].wT * ds; }
+    __shared__ int s_sexp[16];
+    load_scale_exps(ca, s_sexp);
     __syncthreads();
     const T dtT = (T)sc->dt;
     const long long n = sc->n_particles;
@@ -404,7 +410,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
     const bool refl_l = ca.bc[0] == 1, refl_r = ca.bc[1] == 1, refl_t = ca.bc[2] == 1, refl_b = ca.bc[3] == 1;
     unsigned long long segs = 0, killed = 0;
     unsigned flags = 0;
-    T emax = (T)0;
+    int emax_e = kNoExp;
     // Lane state of the history in flight.
     long long i = 0;
     int cs = 0, xi = 0, yi = 0, k = 0, acc_cell = 0;
@@ -476,7 +482,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
             dep = -Edens * m_expm1(-ce.saf * dist);
         }
         if (cell != acc_cell) {
-            flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+            flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep + s_sexp[k], flags);
             acc_s = (T)0; acc_c = (T)0; acc_cell = cell;
         }
         if (newenergy <= minenergy) {
@@ -494,14 +500,14 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
                 if (vx > (T)0) {
                     if (xi == NX - 1) {
                         if (refl_r) { vx = -vx; return 0; }
-                        flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
+                        flush_one<T, false>(ca.lost_acc, k, E, b_lost + s_sexp[k], flags);
                         return 1;
                     }
                     xi += 1; xp = (T)0;
                 } else {
                     if (xi == 0) {
                         if (refl_l) { vx = -vx; return 0; }
-                        flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
+                        flush_one<T, false>(ca.lost_acc, k, E, b_lost + s_sexp[k], flags);
                         return 1;
                     }
                     xi -= 1; xp = fx[xi].ws;
@@ -510,14 +516,14 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
                 if (vy > (T)0) {
                     if (yi == NY - 1) {
                         if (refl_t) { vy = -vy; return 0; }
-                        flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
+                        flush_one<T, false>(ca.lost_acc, k, E, b_lost + s_sexp[k], flags);
                         return 1;
                     }
                     yi += 1; yp = (T)0;
                 } else {
                     if (yi == 0) {
                         if (refl_b) { vy = -vy; return 0; }
-                        flush_one<T, false>(ca.lost_acc, k, E, b_lost, flags);
+                        flush_one<T, false>(ca.lost_acc, k, E, b_lost + s_sexp[k], flags);
                         return 1;
                     }
                     yi -= 1; yp = fy[yi].ws;
@@ -553,14 +559,15 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
                 pb.E[i] = (typename St::S)E;
             }
             if (cellf != (cs & 0xFFFFFF)) pb.cs[i] = cellf | (k << 24);
-            flush_one<T, RAD_SMT>(rad_acc, k * nc + cellf, Est, b_rad, flags);
-            emax = Est > emax ? Est : emax;
+            flush_one<T, RAD_SMT>(rad_acc, k * nc + cellf, Est, b_rad + s_sexp[k], flags);
+            const int ee = exp_bound(Est) - s_sexp[k];
+            emax_e = ee > emax_e ? ee : emax_e;
             return 2;
         }
         return 0;
     };
     auto finish = [&](int end) {
-        flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep, flags);
+        flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep + s_sexp[k], flags);
         if (end == 1) {
             pb.alive[i] = 0;
             ++killed;
@@ -641,7 +648,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
         }
     }
     if (SMT) flush_block_tallies(ca, dep_acc, RAD_SMT);
-    finish_counters<T>(sc, segs, killed, flags, emax);
+    finish_counters(sc, segs, killed, flags, emax_e);
 }
 
 // Launch shape of the transport kernel.  When the table and the block's

@@ -258,25 +258,30 @@ static_assert(sizeof(Tab2<double>) == 16 && sizeof(Tab2<float>) == 16, "16-byte 
 template <class T> struct Face { T ws, wT; };  // width * distancescale, width
 
 // end-of-kernel reduction of per-thread counters: one atomic per warp
-// (segments, histories removed from the list, error flags, census maximum)
-template <class T>
+// (segments, histories removed from the list, error flags, and the census
+// maximum as the exponent of its true energy, see scale_exp)
 __device__ __forceinline__ void finish_counters(Scalars *sc, unsigned long long segs, unsigned long long killed,
-                                                unsigned flags, T emax) {
+                                                unsigned flags, int emax_e) {
     const unsigned full = 0xFFFFFFFFu;
-    double em = (double)emax;
     for (int off = 16; off > 0; off >>= 1) {
         segs += __shfl_down_sync(full, segs, off);
         killed += __shfl_down_sync(full, killed, off);
         flags |= __shfl_down_sync(full, flags, off);
-        double o = __shfl_down_sync(full, em, off);
-        em = o > em ? o : em;
+        const int o = __shfl_down_sync(full, emax_e, off);
+        emax_e = o > emax_e ? o : emax_e;
     }
     if ((threadIdx.x & 31) == 0) {
         if (segs) atomicAdd(&sc->segments, segs);
         if (killed) atomicAdd(&sc->killed, killed);
         if (flags) atomicOr(&sc->flags, flags);
-        if (em > 0.0) atomicMax(&sc->emax_census_bits, (unsigned long long)d2u(em));
+        if (emax_e != kNoExp) atomicMax(&sc->emax_census_exp, emax_e);
     }
+}
+
+// the exponents scale_exp(scale_k) of the deck's energy scales, in shared
+// memory (every thread calls; a barrier must follow before use)
+__device__ __forceinline__ void load_scale_exps(const CellArgs &ca, int *s_sexp) {
+    for (int i = threadIdx.x; i < ca.K; i += blockDim.x) s_sexp[i] = scale_exp(ca.scales[i]);
 }
 
 // ------------------------------------------------ learned surrogate: when to ask

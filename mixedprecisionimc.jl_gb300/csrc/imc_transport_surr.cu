@@ -60,9 +60,11 @@ template <class T> struct Hist {
 };
 
 // census: write the state back (src/imc_transport.jl:185-193) and tally it
+// (b_rad: the census tally's exponent of this history's scale, se that
+// scale's scale_exp)
 template <class St, class T, bool SMT>
 __device__ __forceinline__ void census(PBuf<St> &pb, const Tab1<T> *tab, Hist<T> &h, long long *rad_acc, int nc,
-                                       int b_rad, unsigned &flags, T &emax) {
+                                       int b_rad, int se, unsigned &flags, int &emax_e) {
     const long long i = h.i;
     T Est = h.E;
     if (St::half) {
@@ -80,7 +82,8 @@ __device__ __forceinline__ void census(PBuf<St> &pb, const Tab1<T> *tab, Hist<T>
     }
     if (h.cell != (h.cs & 0xFFFFFF)) pb.cs[i] = h.cell | (h.k << 24);
     flush_one<T, SMT>(rad_acc, h.k * nc + h.cell, Est, b_rad, flags);
-    emax = Est > emax ? Est : emax;
+    const int ee = exp_bound(Est) - se;
+    emax_e = ee > emax_e ? ee : emax_e;
 }
 
 // Face crossing after a segment that ended on a face, in the reference's
@@ -243,6 +246,8 @@ __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scal
         for (int v = threadIdx.x; v < kQueryWarps * kStageFloats; v += blockDim.x) stage_all[v] = 0.0f;
     }
     fill_table<T>(ca, tab, ds);
+    __shared__ int s_sexp[16];
+    load_scale_exps(ca, s_sexp);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
@@ -258,7 +263,7 @@ __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scal
     const bool reflect_r = ca.bc[1] == 1, reflect_l = ca.bc[0] == 1;
     unsigned long long calls = 0, killed = 0;
     unsigned flags = 0;
-    T emax = (T)0;
+    int emax_e = kNoExp;
     const long long wstride = (long long)gridDim.x * kQueryWarps * 32;
     for (long long base = ((long long)blockIdx.x * kQueryWarps + warp) * 32; base < n; base += wstride) {
         const long long e = base + lane;
@@ -291,15 +296,16 @@ __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scal
         if (valid) {
             if (kind == kAsk) {
                 res = apply_outcome<T>(ca, tab, h, q, cls, y0, y1, c, ds, ds_one, dt, cap, N, reflect_l, reflect_r,
-                                       b_lost, flags);
+                                       b_lost + s_sexp[h.k], flags);
                 calls += 1;
             } else if (kind == kCertainKill) {
                 nadd(h.acc_s, h.acc_c, SegMath<T>::all_in(h.E, tab[h.cell]));
                 calls += 1;
                 res = kKilled;
             }
-            flush_pair<T, false>(ca.dep_acc, h.k * nc + h.acc_cell, h.acc_s, h.acc_c, b_dep, flags);
-            if (res == kCensus) census<St, T, false>(pb, tab, h, ca.rad_acc, nc, b_rad, flags, emax);
+            const int se = s_sexp[h.k];
+            flush_pair<T, false>(ca.dep_acc, h.k * nc + h.acc_cell, h.acc_s, h.acc_c, b_dep + se, flags);
+            if (res == kCensus) census<St, T, false>(pb, tab, h, ca.rad_acc, nc, b_rad + se, se, flags, emax_e);
             else if (res == kKilled) {
                 pb.alive[h.i] = 0;
                 ++killed;
@@ -318,7 +324,7 @@ __global__ void __launch_bounds__(kQueryBlock, 2) k_wave_query(CellArgs ca, Scal
     }
     for (int off = 16; off > 0; off >>= 1) calls += __shfl_down_sync(kFull, calls, off);
     if (lane == 0 && calls) atomicAdd(&sc->surrogate_calls, calls);
-    finish_counters<T>(sc, 0ull, killed, flags, emax);
+    finish_counters(sc, 0ull, killed, flags, emax_e);
 }
 
 // BF16 fragment image of FP32 parameters (one block)

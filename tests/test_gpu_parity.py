@@ -246,12 +246,14 @@ def test_multiscale_sorter_fallback_parity(gpu_lib, prec):
     np.testing.assert_allclose(g.field("emittedenergy"), o.field("emittedenergy"), rtol=1e-14)
     _cmp_particles(g, o, rtol=1e-6, keys=("t", "x", "mu", "E", "E0"))
     g, o = _pair("multiscale_1d", gpu_lib, **_MULTISCALE[prec])
-    for _ in range(3):
+    for s in range(3):
         sg, _ = g.step()
         so, _ = o.step()
         assert sg["n_sourced"] == so["n_sourced"]
         assert sg["error_flags"] == 0
-        np.testing.assert_allclose(sg["total_energy"], so["total_energy"], rtol=1e-13)
+        # the first step's energies come from the deck alone; later ones from
+        # temperatures that carry the transports' last-ulp differences
+        np.testing.assert_allclose(sg["total_energy"], so["total_energy"], rtol=1e-13 if s == 0 else 1e-6)
         assert abs(sg["energy_error"] - so["energy_error"]) < 1e-4
     for f in ("temp", "radenergydens", "matenergydens"):
         a, b = g.field(f), o.field(f)
