@@ -472,7 +472,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
         const T dist = jmin(jmin(dist_b, dist_col), dist_cen);
         if (dist != dist) { flags |= 1u; return 1; }
         if constexpr (sizeof(T) == 4) {
-            const float em1 = expm1f(-ce.saf * dist);
+            const float em1 = expm1_seg(-ce.saf * dist);
             newenergy = E + E * em1;
             Edens = E * ce.rarea;
             dep = -Edens * em1;

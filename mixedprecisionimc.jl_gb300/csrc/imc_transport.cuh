@@ -21,6 +21,23 @@ __device__ __forceinline__ double m_abs(double x) { return fabs(x); }
 __device__ __forceinline__ void m_sincos(float a, float *s, float *c) { sincosf(a, s, c); }
 __device__ __forceinline__ void m_sincos(double a, double *s, double *c) { sincos(a, s, c); }
 
+// e^x - 1 in the FP32 segment arithmetic: for |x| <= 1/16 the Taylor series
+// to x^7 in Horner form with fused multiply-adds (the dropped terms are below
+// 1e-13 of the result; rounding within about one ulp), else expm1f.  Segments
+// of sigma_a f d below 1/16 -- every segment of the slab decks -- take the
+// series.  The oracle's FP32 path evaluates the same expression.
+__device__ __forceinline__ float expm1_seg(float x) {
+    if (fabsf(x) <= 0.0625f) {
+        float p = fmaf(x, 1.0f / 5040.0f, 1.0f / 720.0f);
+        p = fmaf(p, x, 1.0f / 120.0f);
+        p = fmaf(p, x, 1.0f / 24.0f);
+        p = fmaf(p, x, 1.0f / 6.0f);
+        p = fmaf(p, x, 0.5f);
+        return fmaf(p * x, x, x);
+    }
+    return expm1f(x);
+}
+
 // Neumaier compensated add; all deposit terms are non-negative.
 template <class T> __device__ __forceinline__ void nadd(T &s, T &c, T x) {
     T t = s + x;
@@ -243,7 +260,7 @@ template <> struct SegMath<float> {
         return -__logf(v) * ce.rseff;
     }
     static __device__ __forceinline__ float attenuate(float E, const Tab1<float> &ce, float d, float *dep) {
-        const float em1 = expm1f(-ce.saf * d);
+        const float em1 = expm1_seg(-ce.saf * d);
         *dep = -(E * ce.rdxT) * em1;
         return E + E * em1;
     }

@@ -40,7 +40,8 @@
  *     formulation of the same quantities: collision distance -log(v)/seff as
  *     -log(v) * (1/seff), the weight after a segment E exp(-a) as
  *     E + E expm1(-a) (the deposit uses the same expm1, so attenuation and
- *     deposit add up to E), and reciprocals of dx and ds*c instead of
+ *     deposit add up to E; expm1 of |a| <= 1/16 as the kernels' Taylor series
+ *     to a^7, expm1_seg), and reciprocals of dx and ds*c instead of
  *     divisions (also 1/mu, set at each new direction, for the face
  *     distance).  They differ from the reference's FP32 evaluation by
  *     roundings only; FP64 keeps the reference's expressions.
@@ -57,6 +58,23 @@
 #include <thread>
 #include <vector>
 #include <chrono>
+
+/* e^x - 1 of the kernels' FP32 segment arithmetic: the Taylor series to x^7
+ * in Horner form with fused multiply-adds for |x| <= 1/16, expm1f beyond. */
+static float expm1_seg(float x) {
+    if (std::fabs(x) <= 0.0625f) {
+        float p = std::fma(x, 1.0f / 5040.0f, 1.0f / 720.0f);
+        p = std::fma(p, x, 1.0f / 120.0f);
+        p = std::fma(p, x, 1.0f / 24.0f);
+        p = std::fma(p, x, 1.0f / 6.0f);
+        p = std::fma(p, x, 0.5f);
+        return std::fma(p * x, x, x);
+    }
+    return std::expm1(x);
+}
+
+/* exported for the CPU test of its error bound */
+extern "C" float orc_expm1_seg(float x) { return expm1_seg(x); }
 
 namespace {
 
@@ -501,7 +519,7 @@ void transport_1d(Sim &s) {
             if (dist != dist) { s.flags |= IMC_FLAG_NAN; p.alive = false; break; }
             T newenergy, dep;
             if (kF32) {
-                const T em1 = std::expm1(-saf[cell] * dist);
+                const T em1 = (T)expm1_seg((float)(-saf[cell] * dist));
                 newenergy = energy + energy * em1;
                 dep = -(energy * rdxT[cell]) * em1;
             } else {
@@ -629,7 +647,7 @@ void transport_2d(Sim &s) {
             const T edens = kF32 ? energy * rarea[cell] : (energy / dxT[xi]) / dyT[yi];
             T newenergy, dep;
             if (kF32) {
-                const T em1 = std::expm1(-saf[cell] * dist);
+                const T em1 = (T)expm1_seg((float)(-saf[cell] * dist));
                 newenergy = energy + energy * em1;
                 dep = -edens * em1;
             } else {

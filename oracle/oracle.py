@@ -61,6 +61,7 @@ def load():
         "orc_bench": (C.c_int, [C.POINTER(ImcDeck), C.c_int, C.c_int64, C.POINTER(C.c_double),
                                 C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
         "orc_surr_walk": (C.c_int, [C.c_uint64, V, C.c_int64, V, V, V]),
+        "orc_expm1_seg": (C.c_float, [C.c_float]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -91,6 +92,11 @@ def surr_walk(seed, state):
     lib.orc_surr_walk(seed, st.ctypes.data_as(C.c_void_p), n, x.ctypes.data_as(C.c_void_p),
                       cls.ctypes.data_as(C.c_void_p), tgt.ctypes.data_as(C.c_void_p))
     return x, cls, tgt
+
+
+def expm1_seg(x):
+    """The FP32 segment arithmetic's e^x - 1 (the kernels' expm1_seg)."""
+    return load().orc_expm1_seg(float(x))
 
 
 def philox_uniforms(seed, step, index, stage, count):

@@ -164,3 +164,16 @@ def test_particle_budget_at_nmax():
     budget = max(2.0, 6000 - nc - 1 - 1)
     # counts round per slot and each cell gets at least CELLMIN=2
     assert born <= budget + 2 * 10 + 2 * 10 + 2 and n1 > 0
+
+
+def test_expm1_segment_series_error_bound():
+    """The FP32 segment arithmetic's e^x - 1 (Taylor series to x^7 for
+    |x| <= 1/16, expm1f beyond) is within 1.5 ulp of e^x - 1 in double."""
+    import math
+    xs = np.concatenate([np.linspace(-0.0625, 0.0625, 4001), -np.logspace(-12, np.log10(0.0625), 2000),
+                         np.logspace(-12, np.log10(0.0625), 2000), [0.0, -0.2, 0.3, -3.0]]).astype(np.float32)
+    for x in xs:
+        got = oracle.expm1_seg(float(x))
+        want = math.expm1(float(x))
+        ulp = float(np.spacing(np.float32(abs(want)))) if want != 0 else 1e-45
+        assert abs(got - want) <= 1.5 * ulp, (float(x), got, want)
