@@ -20,10 +20,14 @@ One bench step is one full simulation (t = 0 -> 3).  Printed on one JSON line:
                the methods at the same statistical error
   fp16_state   one run with binary16 particle state
   learned      the learned thick-cell surrogate (trained first, on the GPU)
-               with FP32 state on the thick-slab deck against plain FP32 and
-               plain FP64, relerr against tests/golden/thick_fp64_mean.npz
+               with FP32 state on the heated thick slab against plain FP32
+               and plain FP64, relerr against the 32-seed FP64 oracle mean
+               (tests/golden/oracle_fp64_ensembles.npz), every arm below 1 %
   c3           the nonlinear heat wave, FP32 state against plain FP64,
                relerr against tests/golden/c3_fp64_mean.npz
+  c4           the 2D channel through thick walls, FP32 state against plain
+               FP64, relerr over the heated cells against
+               tests/golden/c4_fp64_mean.npz, and the 2D transport roofline
   c5           the 256-deck batched ensemble (tests/golden/c5_decks.py) run
                side by side: learned + FP32 and plain FP32 throughput over all
                decks, per-deck error and FOM against plain FP64 on 16 decks
@@ -205,11 +209,32 @@ def run_once(inputs, mesh, overrides=None, timing=False):
         flags |= s["error_flags"]
     moved = sum((s["n_census_in"] + s["n_sourced"]) * READ_B + s["n_census_out"] * WRITE_B for s in steps)
     return {"ms": ms, "segments": segs, "histories": hist, "steps": len(steps), "transport_ms": tr_ms,
+            "balance": balance_forms(steps),
+            "bytes_2d": sum((s["n_census_in"] + s["n_sourced"]) * 33 + s["n_census_out"] * 24 for s in steps),
             "transport_launches": tr_n, "temp": temp, "flags": flags, "bytes": moved, "kernels": kps * len(steps),
             "energy_error": max(abs(s["energy_error"]) for s in steps),
             # the CONSTANT clock's last step is 4.2e-14 long (the reference's
             # N+1-th step); its relative balance divides by ~5e-14 of source
             "energy_error_before_last": max([abs(s["energy_error"]) for s in steps[:-1]] or [0.0])}
+
+
+def balance_forms(steps):
+    """The energy balance of src/imc_energycheck.jl:34 per step in two forms:
+    relative to the step's source energy (the reference's; ill-conditioned on
+    the CONSTANT clock's last step, 4.2e-14 long on the slab, whose source is
+    ~1e-11 of the census energy), and relative to all the energy in play that
+    step (source + census carried in), well conditioned on every step.  Also
+    the binary16 rounding bound of FP16 state: census energies are stored as
+    E/E0 in binary16, so each step's balance may miss up to 2^-11 of the
+    census energy (relative to the source energy: 2^-11 E_rad / E_src)."""
+    ref = max(abs(s["energy_error"]) for s in steps)
+    wc = max(abs(s["energy_error"] * s["total_energy"]) / (s["total_energy"] + s["rad_energy_old"])
+             for s in steps)
+    bound16 = max(2.0 ** -11 * s["rad_energy"] / s["total_energy"] for s in steps)
+    worst16 = max(abs(s["energy_error"]) / (2.0 ** -11 * s["rad_energy"] / s["total_energy"] + 1e-7)
+                  for s in steps)
+    return {"reference_form_max": ref, "in_play_form_max": wc, "fp16_rounding_bound_max": bound16,
+            "fp16_error_over_bound_max": worst16}
 
 
 def deck_runs(deck_file, offsets, overrides=None, params=None):
@@ -253,27 +278,49 @@ def fp64_ref(name):
     return np.load(os.path.join(GOLDEN, name + "_fp64_mean.npz"))
 
 
-def learned_section(n):
-    """The learned part on the thick-slab deck (40 mean free paths per cell):
-    learned surrogate + FP32 state against plain FP32 and plain FP64, each
-    against the 32-seed FP64 mean; the network is trained here first."""
+def learned_section(n, n64=8):
+    """The learned part on the heated thick slab (tests/golden/decks/
+    thick_heated.txt: 30 cells of 40 mean free paths, a source in every cell,
+    vacuum on the right): learned surrogate + FP32 state against plain FP32
+    and plain FP64, each run's temperature error against the 32-seed FP64
+    oracle mean of the same deck (tests/golden/oracle_fp64_ensembles.npz),
+    where every arm's error is below 1 %.  Seeds are paired (run i of every
+    arm uses seed SEED + i), so per-run FOM ratios show the spread.  The
+    network is trained here first, on the GPU."""
+    import numpy as np
     from mpimc import surrogate
     t0 = time.perf_counter()
     P = surrogate.train()
     train_s = time.perf_counter() - t0
-    ref = fp64_ref("thick")
-    learned = summarize(deck_runs("thick_slab.txt", range(1, n + 1), None, P), ref)
-    fp32 = summarize(deck_runs("thick_slab.txt", range(1, n + 1)), ref)
-    fp64 = summarize(deck_runs("thick_slab.txt", range(1, n + 1), {"precision": 0, "scale_select_precision": 0}),
-                     ref)
-    return {"deck": "thick_slab.txt",
-            "workload": "1D linearized thick slab, 30 cells of 40 mean free paths (sigma_a=800, dx=0.05), "
-                        "source on [0,0.5], dt=0.5 to t=10, NINPUT=2e5, NMAX=2e6",
-            "train_s": train_s, "train": dict(surrogate.DEFAULT_TRAIN),
-            "learned_fp32": learned, "fp32": fp32, "fp64": fp64,
-            "fom_ratio_learned_over_fp64": learned["fom"] / fp64["fom"],
-            "fom_ratio_learned_over_fp32": learned["fom"] / fp32["fom"],
-            "segment_ratio_fp32_over_learned": fp32["segments_per_run"] / learned["segments_per_run"]}
+    ens = np.load(os.path.join(GOLDEN, "oracle_fp64_ensembles.npz"))
+    if "thick_temp" not in ens.files:
+        return {"deck": "thick_heated.txt", "error": "oracle ensemble of the deck not generated"}
+    ref = {"temp": ens["thick_temp"]}
+    fp64_ov = {"precision": 0, "scale_select_precision": 0}
+    arms = {"learned_fp32": deck_runs("thick_heated.txt", range(1, n + 1), None, P),
+            "fp32": deck_runs("thick_heated.txt", range(1, n + 1)),
+            "fp64": deck_runs("thick_heated.txt", range(1, n64 + 1), fp64_ov)}
+    out = {"deck": "thick_heated.txt",
+           "workload": "1D linearized thick slab, 30 cells of 40 mean free paths (sigma_a=800, dx=0.05), "
+                       "source 1.0 in every cell, reflect left / vacuum right, dt=0.5 to t=10, NINPUT=2e5, NMAX=2e6",
+           "error_reference": "32-seed FP64 oracle mean (CPU restatement), tests/golden/oracle_fp64_ensembles.npz",
+           "train_s": train_s, "train": dict(surrogate.DEFAULT_TRAIN)}
+    for k, runs in arms.items():
+        out[k] = summarize(runs, ref)
+        out[k]["relerr_T_each"] = [relerr(r["temp"], ref) for r in runs]
+        out[k]["ms_each"] = [r["ms"] for r in runs]
+    fom_each = lambda k: [1.0 / (e ** 2 * m / 1000.0) for e, m in zip(out[k]["relerr_T_each"], out[k]["ms_each"])]
+    fl, f32, f64 = fom_each("learned_fp32"), fom_each("fp32"), fom_each("fp64")
+    pair64 = [a / b for a, b in zip(fl, f64)]
+    pair32 = [a / b for a, b in zip(fl, f32)]
+    out["fom_ratio_learned_over_fp64"] = out["learned_fp32"]["fom"] / out["fp64"]["fom"]
+    out["fom_ratio_learned_over_fp32"] = out["learned_fp32"]["fom"] / out["fp32"]["fom"]
+    out["fom_ratio_learned_over_fp64_paired"] = {"median": float(np.median(pair64)), "min": float(np.min(pair64)),
+                                                 "max": float(np.max(pair64)), "pairs": len(pair64)}
+    out["fom_ratio_learned_over_fp32_paired"] = {"median": float(np.median(pair32)), "min": float(np.min(pair32)),
+                                                 "max": float(np.max(pair32)), "pairs": len(pair32)}
+    out["segment_ratio_fp32_over_learned"] = out["fp32"]["segments_per_run"] / out["learned_fp32"]["segments_per_run"]
+    return out
 
 
 def c3_section(n):
@@ -286,6 +333,66 @@ def c3_section(n):
                      ref)
     return {"deck": "c3_heatwave.txt", "workload": DECKS["c3"][1], "fp32": fp32, "fp64": fp64,
             "fom_ratio_fp32_over_fp64": fp32["fom"] / fp64["fom"]}
+
+
+def c4_section(n32=2, n64=2):
+    """The 2D channel through thick walls (BASELINE's 2D configuration,
+    tests/golden/decks/c4_channel2d.txt): FP32 state against plain FP64, each
+    run's temperature error over the heated cells (reference mean above
+    1.05 T_init) against the 8-seed GPU FP64 mean tests/golden/c4_fp64_mean.npz
+    (the GPU FP64 path is tied to the oracle per history and by the
+    reduced-channel ensemble test); the 2D transport kernel's roofline from
+    one instrumented FP32 run."""
+    import numpy as np
+    import mpimc
+    deck = os.path.join(GOLDEN, "decks", DECKS["c4"][0])
+    refp = os.path.join(GOLDEN, "c4_fp64_mean.npz")
+    ref = np.load(refp)["temp"] if os.path.exists(refp) else None
+
+    def runs(ov, n, timing=False):
+        out = []
+        for i in range(n):
+            inputs = mpimc.Input.readInputs(deck)
+            inputs["SEED"] = str(int(inputs["SEED"]) + 1 + i)
+            mesh = mpimc.Mesh.mesh_generation(inputs)
+            out.append(run_once(inputs, mesh, ov, timing=timing))
+        return out
+
+    def err(temp):
+        if ref is None:
+            return None
+        live = ref > 1.05 * 0.05
+        return float(np.sqrt(np.mean(((temp[live] - ref[live]) / ref[live]) ** 2)))
+
+    def arm(rs):
+        secs = sum(r["ms"] for r in rs) / 1000.0 / len(rs)
+        e = [err(r["temp"]) for r in rs]
+        rel = None if e[0] is None else float(np.sqrt(np.mean(np.square(e))))
+        return {"runs": len(rs), "ms_per_run": 1000.0 * secs, "relerr_T": rel, "relerr_T_each": e,
+                "fom": None if rel is None else 1.0 / (rel ** 2 * secs),
+                "segments_per_s": sum(r["segments"] for r in rs) / (secs * len(rs)),
+                "energy_error_max": max(r["energy_error"] for r in rs),
+                "kernels_per_run": rs[0]["kernels"]}
+
+    f32 = arm(runs(None, n32))
+    f64 = arm(runs({"precision": 0, "scale_select_precision": 0}, n64))
+    inst = runs(None, 1, timing=True)[0]
+    peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+    hbm = peaks.get("hbm_gbs")
+    n_l = max(inst["transport_launches"], 1)
+    bpl = inst["bytes_2d"] / n_l
+    ach = bpl / (inst["transport_ms"] / 1000.0) / 1e9 if inst["transport_ms"] > 0 else None
+    out = {"deck": DECKS["c4"][0], "workload": DECKS["c4"][1], "fp32": f32, "fp64": f64,
+           "error_reference": "8-seed GPU FP64 mean (tests/golden/c4_fp64_mean.npz), heated cells",
+           "roofline_k_transport2d": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                                      "frac": (ach / hbm) if (ach and hbm) else None,
+                                      "avg_launch_ms": inst["transport_ms"], "launches": inst["transport_launches"],
+                                      "algorithmic_bytes_per_launch": bpl,
+                                      "transport_share_of_step": inst["transport_ms"] * n_l / inst["ms"]}}
+    if f32["fom"] and f64["fom"]:
+        out["fom_ratio_fp32_over_fp64"] = f32["fom"] / f64["fom"]
+    out["time_ratio_fp64_over_fp32"] = f64["ms_per_run"] / f32["ms_per_run"]
+    return out
 
 
 def c5_section(n_err=16):
@@ -465,6 +572,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-surrogate comparison (thick slab)")
     ap.add_argument("--no-c3", action="store_true", help="skip the nonlinear heat-wave FP32 / FP64 comparison")
     ap.add_argument("--no-c5", action="store_true", help="skip the 256-deck batched ensemble")
+    ap.add_argument("--no-c4", action="store_true", help="skip the 2D channel FP32 / FP64 comparison")
     ap.add_argument("--profile", action="store_true",
                     help="profiling case for ncu: the deck at half the particle counts, 12 timesteps, then exit")
     ap.add_argument("--profile-learned", action="store_true",
@@ -493,14 +601,16 @@ def main():
     hbm = peaks.get("hbm_gbs")
     inputs, mesh = load_deck(rank)
     for _ in range(args.warmup):
-        run_once(inputs, mesh, timing=True)
+        run_once(inputs, mesh)
     if dist:
         dist.barrier()
     runs = []
+    # the timed runs replay each step's captured CUDA graph (the product's
+    # path, imc_run); device time from CUDA events around the whole run
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         for i in range(args.steps):
-            runs.append(run_once(*load_deck(rank + 1000 * (i + 1)), timing=True))
+            runs.append(run_once(*load_deck(rank + 1000 * (i + 1))))
         wall = time.perf_counter() - t0
     dev_ms = sum(r["ms"] for r in runs)
     segs = sum(r["segments"] for r in runs)
@@ -517,10 +627,13 @@ def main():
         rel += [relerr(run_once(*load_deck(1000 * (i + 1)))["temp"], ref) for i in range(len(runs), N_ERR_FP32)]
     rel_m = None if rel[0] is None else float(np.sqrt(np.mean(np.square(rel))))
     fom = None if rel_m is None else 1.0 / (rel_m ** 2 * s_per_run)
-    # roofline of the transport kernel
-    tr_ms = sum(r["transport_ms"] * r["transport_launches"] for r in runs)
-    tr_n = sum(r["transport_launches"] for r in runs)
-    bytes_per_launch = sum(r["bytes"] for r in runs) / max(tr_n, 1)
+    # roofline of the transport kernel, from a separate instrumented run of
+    # the same deck: per-launch CUDA events around each transport launch
+    # (direct launches, no graph), on the handle's stream
+    inst = run_once(*load_deck(rank + 999), timing=True)
+    tr_ms = inst["transport_ms"] * inst["transport_launches"]
+    tr_n = inst["transport_launches"]
+    bytes_per_launch = inst["bytes"] / max(tr_n, 1)
     avg_ms = tr_ms / max(tr_n, 1)
     achieved = bytes_per_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -531,7 +644,9 @@ def main():
                                   "algorithmic bytes",
                 "kernel": "k_transport2d<StF32>" if DECK_KEY == "c4" else "k_transport1d<StF32>", "avg_launch_ms": avg_ms, "launches": tr_n,
                 "algorithmic_bytes_per_launch": bytes_per_launch,
-                "transport_share_of_step": tr_ms / dev_ms if dev_ms else None,
+                "transport_share_of_step": tr_ms / inst["ms"] if inst["ms"] else None,
+                "timing": "separate instrumented run (per-launch CUDA events, direct launches); the timed "
+                          "runs replay CUDA graphs",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"}
     out = {
         "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": world, "steps": args.steps,
@@ -544,6 +659,7 @@ def main():
         "relerr_T": rel_m, "relerr_runs": len(rel), "fom": fom,
         "energy_error_max": max(r["energy_error"] for r in runs),
         "energy_error_max_before_last_step": max(r["energy_error_before_last"] for r in runs),
+        "energy_error_in_play_max": max(r["balance"]["in_play_form_max"] for r in runs),
         "error_flags": int(np.bitwise_or.reduce([r["flags"] for r in runs])),
         "gpu_launches": sum(r["kernels"] for r in runs),
         "clocks": clk.summary(),
@@ -562,7 +678,10 @@ def main():
         return {"value": sum(r["segments"] for r in rs) / secs, "unit": "segments/s", "runs": n,
                 "ms_per_step": 1000.0 * secs / n, "relerr_T": rel_c, "fom": fom_c,
                 "energy_error_max": max(r["energy_error"] for r in rs),
-                "energy_error_max_before_last_step": max(r["energy_error_before_last"] for r in rs)}
+                "energy_error_max_before_last_step": max(r["energy_error_before_last"] for r in rs),
+                "energy_error_in_play_max": max(r["balance"]["in_play_form_max"] for r in rs),
+                "fp16_rounding_bound_max": max(r["balance"]["fp16_rounding_bound_max"] for r in rs),
+                "fp16_error_over_bound_max": max(r["balance"]["fp16_error_over_bound_max"] for r in rs)}
 
     if not args.no_fp64:
         # the plain FP64 GPU path, as many runs as the timed FP32 runs
@@ -576,11 +695,16 @@ def main():
         out["learned"] = learned_section(max(args.steps, 4))
     if not args.no_c3:
         out["c3"] = c3_section(2)
+    if not args.no_c4 and DECK_KEY != "c4":
+        out["c4"] = c4_section()
     if not args.no_c5:
         out["c5"] = c5_section()
-    w, s, h2d, d2h = e2e_once(2000)
-    out["e2e"] = {"value": s / w, "unit": "segments/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                  "wall_s_per_step": w}
+    e2e = [e2e_once(2000 + i) for i in range(3)]
+    w = sum(x[0] for x in e2e) / len(e2e)
+    s_e = sum(x[1] for x in e2e) / len(e2e)
+    out["e2e"] = {"value": s_e / w, "unit": "segments/s", "h2d_bytes_per_step": e2e[0][2],
+                  "d2h_bytes_per_step": e2e[0][3], "wall_s_per_step": w, "runs": len(e2e),
+                  "wall_s_each": [x[0] for x in e2e]}
     if not args.no_cpu:
         try:
             out["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1)
