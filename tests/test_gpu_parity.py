@@ -138,15 +138,38 @@ def test_step_parity_fp32_2d(gpu_lib):
 
 
 def test_energy_conservation_fp64(gpu_lib):
-    """src/imc_energycheck.jl:34 balance: <= 1e-10 relative in FP64 (1D, no
-    2D source quirk)."""
+    """src/imc_energycheck.jl:34 balance in FP64 over the whole C1 run.  In the
+    reference's form (relative to the step's source energy) <= 1e-10 on every
+    step but the CONSTANT clock's last one, whose dt is a rounding residue
+    of t_end and whose source is a vanishing fraction of the energy in play;
+    relative to all the energy in play (source + census carried in) <= 1e-12
+    on every step, the last included."""
     import mpimc
     inputs, mesh = load_deck("c1_slab")
     g = mpimc.Engine(inputs, mesh)
-    steps, _ = g.run(max_steps=40)
-    assert len(steps) == 40
+    steps, _ = g.run()
+    assert len(steps) == 101
     for s in steps:
-        assert abs(s["energy_error"]) <= 1e-10, s
+        in_play = abs(s["energy_error"] * s["total_energy"]) / (s["total_energy"] + s["rad_energy_old"])
+        assert in_play <= 1e-12, s
+        if s["dt"] > 1e-9 * 0.01:
+            assert abs(s["energy_error"]) <= 1e-10, s
+
+
+def test_fp16_state_balance_within_storage_rounding(gpu_lib):
+    """FP16 particle state stores each census energy as E/E0 in binary16, so a
+    step's balance misses at most the rounding of the census energy:
+    |error| <= 2^-11 E_rad / E_src (plus the FP32 arithmetic's 1e-6)."""
+    import mpimc
+    inputs, mesh = load_deck("c1_slab", PRECISION=np.float16)
+    g = mpimc.Engine(inputs, mesh)
+    steps, _ = g.run(max_steps=60)
+    worst = 0.0
+    for s in steps:
+        bound = 2.0 ** -11 * s["rad_energy"] / s["total_energy"] + 1e-6
+        assert abs(s["energy_error"]) <= bound, s
+        worst = max(worst, abs(s["energy_error"]) / bound)
+    assert worst > 0.0
 
 
 def test_run_matches_step(gpu_lib):
