@@ -520,6 +520,15 @@ int imc_create(const ImcDeck *d, ImcHandle **out) {
     double *p;
     if ((rc = upload(h, &p, d->dx, h->nx))) return bail(rc); ca.dx = p;
     if ((rc = upload(h, &p, d->geometry == IMC_GEOM_2D ? d->dy : ones.data(), h->ny))) return bail(rc); ca.dy = p;
+    {
+        // binary32 copies of the widths for the FP32 / FP16 births
+        std::vector<float> wf(d->dx, d->dx + h->nx);
+        float *fp;
+        if ((rc = upload(h, &fp, wf.data(), h->nx))) return bail(rc); ca.dxf = fp;
+        wf.assign(h->ny, 1.0f);
+        if (d->geometry == IMC_GEOM_2D) for (int j = 0; j < h->ny; ++j) wf[j] = (float)d->dy[j];
+        if ((rc = upload(h, &fp, wf.data(), h->ny))) return bail(rc); ca.dyf = fp;
+    }
     if ((rc = upload(h, &ca.temp, d->temp, nc))) return bail(rc);
     if ((rc = upload(h, &ca.bee, d->bee, nc))) return bail(rc);
     if ((rc = upload(h, &ca.beta, ones.data(), nc))) return bail(rc);
@@ -544,6 +553,7 @@ int imc_create(const ImcDeck *d, ImcHandle **out) {
     if ((rc = upload<double>(h, &ca.slot_e, nullptr, h->nslots))) return bail(rc);
     if ((rc = upload<double>(h, &ca.slot_s, nullptr, h->nslots))) return bail(rc);
     if ((rc = upload<double>(h, &ca.slot_nrg, nullptr, h->nslots))) return bail(rc);
+    if ((rc = upload<float>(h, &ca.slot_nrg_f, nullptr, h->nslots))) return bail(rc);
     if ((rc = upload<int>(h, &ca.slot_j, nullptr, h->nslots))) return bail(rc);
     if ((rc = upload<long long>(h, &ca.slot_n, nullptr, h->nslots))) return bail(rc);
     if ((rc = upload<long long>(h, &ca.slot_off, nullptr, h->nslots))) return bail(rc);

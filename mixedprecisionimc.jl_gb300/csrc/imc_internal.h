@@ -65,6 +65,8 @@ struct CellArgs {
     // sourcing scratch (per source slot)
     int nslots;
     double *slot_e, *slot_s, *slot_nrg, *slot_q;
+    float *slot_nrg_f;                 // slot_nrg rounded to binary32 (FP32 / FP16 births)
+    const float *dxf, *dyf;            // cell widths rounded to binary32 (FP32 / FP16 births)
     int *slot_j;
     long long *slot_n, *slot_off;
     // per-block partial sums (double-double pairs) and maxima

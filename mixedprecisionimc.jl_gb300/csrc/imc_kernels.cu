@@ -284,6 +284,7 @@ __global__ void __launch_bounds__(kCellThreads) k_source_counts(CellArgs ca, Sca
         const double nrg = n > 0 ? e[q] / (double)nd : 0.0;
         ca.slot_n[q] = n;
         ca.slot_nrg[q] = nrg;
+        ca.slot_nrg_f[q] = (float)nrg;
         // the largest birth energy in true units (see scale_exp)
         if (n > 0) my = ldexp(nrg, -scale_exp(ca.scales[ca.slot_j[q]]));
     }
@@ -431,7 +432,7 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
         const long long pid = n_census + j;
         Stream rs;
         rs.init(ca.seed, step, (uint32_t)pid, kStageSource);
-        const T E0 = (T)ca.slot_nrg[q];
+        const T E0 = sizeof(T) == 4 ? (T)ca.slot_nrg_f[q] : (T)ca.slot_nrg[q];
         const int k = ca.slot_j[q] < 0 ? 0 : ca.slot_j[q];
         if (ca.geometry == 1) {
             if (q < 2) {
@@ -450,7 +451,7 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
             } else {
                 // body / source births (src/imc_sourcing.jl:193-236)
                 const int cell = q < ns + nc ? q - ns : q - ns - nc;
-                T xpos = (T)ca.dx[cell] * Rand<T>::u(rs) * dsT;
+                T xpos = (sizeof(T) == 4 ? (T)ca.dxf[cell] : (T)ca.dx[cell]) * Rand<T>::u(rs) * dsT;
                 T mu = (T)0;
                 for (int r = 0; r < 64 && mu == (T)0; ++r) mu = (T)1 - (T)2 * Rand<T>::u(rs);
                 if (mu == (T)0) mu = (T)1;
@@ -472,11 +473,17 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
                 if (face < 2) {
                     ix = idx;
                     iy = face == 0 ? 0 : ny - 1;
-                    xpos = (T)ca.dx[ix] * Rand<T>::u(rs) * dsT;
+                    xpos = (sizeof(T) == 4 ? (T)ca.dxf[ix] : (T)ca.dx[ix]) * Rand<T>::u(rs) * dsT;
                     ypos = face == 0 ? (T)(0.001 * (double)(T)ca.dy[0] * (double)dsT)
                                      : (T)(0.999 * (double)(T)ca.dy[ny - 1] * (double)dsT);
-                    T u = Rand<T>::u(rs);
-                    ang = face == 0 ? (T)((T)pd * u) : (T)(-pd * (double)u);
+                    if constexpr (sizeof(T) == 4) {
+                        // -pi u in Float64, rounded to binary32 (integer form, f32_of_f64_product)
+                        const uint32_t m = rs.next() >> 8;
+                        ang = face == 0 ? (T)((T)pd * ((float)m * 0x1p-24f)) : -f32_of_f64_product(kTwoPiM, kTwoPiE - 1, m);
+                    } else {
+                        T u = Rand<T>::u(rs);
+                        ang = face == 0 ? (T)((T)pd * u) : (T)(-pd * (double)u);
+                    }
                 } else {
                     iy = idx;
                     ix = face == 2 ? 0 : nx - 1;
@@ -485,17 +492,33 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
                     // the reference scales y by mesh.dx[j] (src/imc_sourcing.jl:301,316)
                     const double wq = iy < nx ? ca.dx[iy] : ca.dy[iy];
                     ypos = (T)wq * Rand<T>::u(rs) * dsT;
-                    T u = Rand<T>::u(rs);
-                    ang = face == 2 ? (T)(pd * (0.5 - (double)u)) : (T)(pd * (0.5 + (double)u));
+                    if constexpr (sizeof(T) == 4) {
+                        // pi (0.5 -+ u) in Float64: (0.5 -+ u) = (2^23 -+ m) 2^-24 exactly
+                        const uint32_t m = rs.next() >> 8;
+                        const uint32_t h23 = 1u << 23;
+                        if (face == 2) ang = m <= h23 ? f32_of_f64_product(kTwoPiM, kTwoPiE - 1, h23 - m)
+                                                      : -f32_of_f64_product(kTwoPiM, kTwoPiE - 1, m - h23);
+                        else ang = f32_of_f64_product(kTwoPiM, kTwoPiE - 1, h23 + m);
+                    } else {
+                        T u = Rand<T>::u(rs);
+                        ang = face == 2 ? (T)(pd * (0.5 - (double)u)) : (T)(pd * (0.5 + (double)u));
+                    }
                 }
             } else {
                 // body / source births (src/imc_sourcing.jl:326-366)
                 const int cell = q < ns + nc ? q - ns : q - ns - nc;
                 ix = cell % ca.nx;
                 iy = cell / ca.nx;
-                xpos = (T)ca.dx[ix] * Rand<T>::u(rs) * dsT;
-                ypos = (T)ca.dy[iy] * Rand<T>::u(rs) * dsT;
-                ang = (T)(2.0 * pd * (double)Rand<T>::u(rs));
+                if constexpr (sizeof(T) == 4) {
+                    // the widths and 2 pi u in Float64 rounded to binary32, without FP64 operations
+                    xpos = (T)ca.dxf[ix] * Rand<T>::u(rs) * dsT;
+                    ypos = (T)ca.dyf[iy] * Rand<T>::u(rs) * dsT;
+                    ang = f32_of_f64_product(kTwoPiM, kTwoPiE, rs.next() >> 8);
+                } else {
+                    xpos = (T)ca.dx[ix] * Rand<T>::u(rs) * dsT;
+                    ypos = (T)ca.dy[iy] * Rand<T>::u(rs) * dsT;
+                    ang = (T)(2.0 * pd * (double)Rand<T>::u(rs));
+                }
                 st = dtT * Rand<T>::u(rs);
             }
             T ux, uy;
