@@ -210,6 +210,7 @@ def run_once(inputs, mesh, overrides=None, timing=False):
     moved = sum((s["n_census_in"] + s["n_sourced"]) * READ_B + s["n_census_out"] * WRITE_B for s in steps)
     return {"ms": ms, "segments": segs, "histories": hist, "steps": len(steps), "transport_ms": tr_ms,
             "balance": balance_forms(steps),
+            "fp16_over_bound_before_last": balance_forms(steps[:-1] or steps)["fp16_error_over_bound_max"],
             "bytes_2d": sum((s["n_census_in"] + s["n_sourced"]) * 33 + s["n_census_out"] * 24 for s in steps),
             "transport_launches": tr_n, "temp": temp, "flags": flags, "bytes": moved, "kernels": kps * len(steps),
             "energy_error": max(abs(s["energy_error"]) for s in steps),
@@ -680,8 +681,8 @@ def main():
                 "energy_error_max": max(r["energy_error"] for r in rs),
                 "energy_error_max_before_last_step": max(r["energy_error_before_last"] for r in rs),
                 "energy_error_in_play_max": max(r["balance"]["in_play_form_max"] for r in rs),
-                "fp16_rounding_bound_max": max(r["balance"]["fp16_rounding_bound_max"] for r in rs),
-                "fp16_error_over_bound_max": max(r["balance"]["fp16_error_over_bound_max"] for r in rs)}
+                **({"fp16_error_over_rounding_bound_max_before_last_step":
+                    max(r["fp16_over_bound_before_last"] for r in rs)} if prec_code == 2 else {})}
 
     if not args.no_fp64:
         # the plain FP64 GPU path, as many runs as the timed FP32 runs
