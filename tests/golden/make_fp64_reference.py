@@ -7,6 +7,11 @@ relative temperature error of its runs against these means.
 
     python tests/golden/make_fp64_reference.py c3_heatwave c3 [n_seeds]
     python tests/golden/make_fp64_reference.py thick_slab thick [n_seeds]
+    python tests/golden/make_fp64_reference.py c4_channel2d c4 8
+
+(c4_fp64_mean.npz: 8 seeds of the full 140 x 40 channel, 112 s on one GB300;
+the GPU FP64 channel is tied to the oracle by the reduced-channel ensemble
+test.)
 
 (deck file tests/golden/decks/<deck>.txt; output <name>_fp64_mean.npz)
 """
