@@ -587,6 +587,7 @@ int imc_create(const ImcDeck *d, ImcHandle **out) {
     // scalars
     Scalars sc{};
     sc.emax_census_exp = kNoExp;
+    sc.surr_gate = 1;
     h->t = 0.0;
     h->dt = d->timestepping == IMC_TS_RAMP ? d->dt0 : d->dt;
     sc.t = h->t; sc.dt = h->dt;
@@ -610,6 +611,7 @@ int imc_create(const ImcDeck *d, ImcHandle **out) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp, h->block_transport, smem) != cudaSuccess || per_sm < 1)
         return bail(fail(h, IMC_ERR_CUDA, "transport kernel cannot be resident"));
     h->grid_full = h->sm_count * per_sm;
+    ca.surr_min_calls = 2ll * h->sm_count * 1024;  // two queries per thread of the GPU
     h->grid_transport = sized_grid(h, h->grid_full, h->block_transport);
     h->grid_emit = h->sm_count * 4;
     if (cudaEventCreate(&h->ev[0]) != cudaSuccess || cudaEventCreate(&h->ev[1]) != cudaSuccess)

@@ -23,6 +23,7 @@
 namespace imc {
 
 // query rounds per step of the surrogate transport (launch_transport_surr)
+constexpr unsigned kSurrProbe = 32;  // steps between re-openings of the surrogate gate (k_energycheck)
 constexpr int kSurrRounds = 1;  // measured best on GB300 (thick slab: 1 round 84 ms, 3 rounds 104 ms, 6 rounds 134 ms)
 
 // scalars that live in device memory so a whole step can replay as a graph
@@ -53,6 +54,7 @@ struct Scalars {
     int cur;                           // particle buffer holding the list (0 or 1)
     int compact_src;                   // buffer compacted from this step
     int compact_now;                   // this step compacts the list
+    int surr_gate;                     // learned surrogate: this step may set histories aside
 };
 
 struct CellArgs {
@@ -85,6 +87,7 @@ struct CellArgs {
     // learned thick-cell surrogate: tensor-core image of the network
     // (imc_surrogate.cuh), or null for analog transport everywhere
     const uint4 *surr_image;
+    long long surr_min_calls;          // queries a step needs to keep the network on (surr_gate)
 };
 
 // type-erased particle buffer

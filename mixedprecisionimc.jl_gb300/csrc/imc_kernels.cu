@@ -913,6 +913,18 @@ __global__ void __launch_bounds__(544) k_energycheck(CellArgs ca, Scalars *sc, D
     sc->radenergy = radenergy;
     sc->radenergyold = radenergy;
     sc->lostenergy = 0.0;
+    // Learned surrogate gate for the next step.  Its extra passes (a query
+    // pass and an analog resume pass after the list pass) pay only when a
+    // step holds enough queries to fill the GPU about twice over; with
+    // fewer, the passes' latency outweighs the collisions the queries save
+    // (measured on the 256-deck ensemble).  A step that ran with the gate
+    // open keeps it open only if it made ca.surr_min_calls queries; every
+    // kSurrProbe-th step opens it again to measure.  The decision uses the
+    // step's own counts, so runs stay reproducible.
+    if (ca.surr_image) {
+        if (sc->surr_gate) sc->surr_gate = (long long)sc->surrogate_calls >= ca.surr_min_calls ? 1 : 0;
+        if ((sc->step + 1u) % kSurrProbe == 0u) sc->surr_gate = 1;
+    }
     if (STEP) advance_clock(ca, sc);  // the step sequence: timestep in the same launch
 }
 

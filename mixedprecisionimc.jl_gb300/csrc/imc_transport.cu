@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     // block fills the whole gate, so all blocks agree): if none is, no
     // history is tested
     bool gating = false;
-    if (kPause) gating = __syncthreads_or(gate_open(ca, gate));
+    if (kPause) gating = __syncthreads_or(gate_open(ca, gate)) && sc->surr_gate != 0;
     else __syncthreads();
     const int b_dep = sc->b_dep, b_rad = sc->b_rad, b_lost = sc->b_lost;
     const unsigned step = sc->step;
