@@ -55,6 +55,7 @@ struct Scalars {
     int compact_src;                   // buffer compacted from this step
     int compact_now;                   // this step compacts the list
     int surr_gate;                     // learned surrogate: this step may set histories aside
+    long long surr_closed_h;           // histories of the step that last closed the gate
 };
 
 struct CellArgs {

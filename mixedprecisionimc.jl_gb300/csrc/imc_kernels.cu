@@ -918,11 +918,19 @@ __global__ void __launch_bounds__(544) k_energycheck(CellArgs ca, Scalars *sc, D
     // step holds enough queries to fill the GPU about twice over; with
     // fewer, the passes' latency outweighs the collisions the queries save
     // (measured on the 256-deck ensemble).  A step that ran with the gate
-    // open keeps it open only if it made ca.surr_min_calls queries; every
-    // kSurrProbe-th step opens it again to measure.  The decision uses the
-    // step's own counts, so runs stay reproducible.
+    // open keeps it open only if it made ca.surr_min_calls queries.  A
+    // closed gate opens again to measure when the step's histories have
+    // doubled since it closed (a census still filling up) and every
+    // kSurrProbe-th step.  The decision uses the step's own counts, so runs
+    // stay reproducible.
     if (ca.surr_image) {
-        if (sc->surr_gate) sc->surr_gate = (long long)sc->surrogate_calls >= ca.surr_min_calls ? 1 : 0;
+        const long long hist = sc->n_census_in + sc->n_sourced;
+        if (sc->surr_gate) {
+            sc->surr_gate = (long long)sc->surrogate_calls >= ca.surr_min_calls ? 1 : 0;
+            if (!sc->surr_gate) sc->surr_closed_h = hist;
+        } else if (hist >= 2 * sc->surr_closed_h) {
+            sc->surr_gate = 1;
+        }
         if ((sc->step + 1u) % kSurrProbe == 0u) sc->surr_gate = 1;
     }
     if (STEP) advance_clock(ca, sc);  // the step sequence: timestep in the same launch
