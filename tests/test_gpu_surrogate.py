@@ -137,3 +137,52 @@ def test_trained_outcomes_match_analog_walks(surrogate_params):
             dw = tw[cw == S.TRUNC, 0].mean()
             ds = y0[cs == S.TRUNC].mean()
             assert abs(dw - ds) < 0.1 + 0.1 * abs(dw), (case, dw, ds)
+
+
+@pytest.mark.parametrize("dn,mup", [(6.0, 0.4), (15.0, -0.7), (2.0, 0.9)])
+def test_walk_generator_equals_transport_kernel_walks(gpu_lib, dn, mup):
+    """The training walks (imc_surrogate_walk) are the plain transport kernel's
+    in-cell walks: 200,000 histories started in one state inside a thick cell
+    (tests/golden/decks/walk_cell.txt: 40 mean free paths of effective scatter,
+    lmax = the census path, 399 mean free paths) and moved by the FP32
+    transport kernel, against 200,000 generator walks from the same
+    (d_n, d_f, mu', lmax).  A history that leaves the cell reaches census in
+    the transparent buffer on its side, so the census cell gives the exit
+    face and the census direction the exit |mu|.  Outcome fractions agree
+    within 4 binomial sigma, mean exit |mu| and mean ln(exit path / lmax)
+    within 4 sigma."""
+    import mpimc
+    from mpimc import surrogate as G
+    from conftest import load_deck
+    inputs, mesh = load_deck("walk_cell", NMAX="400000")
+    e = mpimc.Engine(inputs, mesh)
+    e.update()
+    f, sa = e.field("fleck")[1], e.field("sigma_a")[1]
+    seff = sa * (1.0 - f)
+    W = 0.05 * seff
+    lmax = 0.5 * seff  # c dt seff, from t = 0; the cut-off path is ~4.6x longer
+    n = 200000
+    e.set_particles({"t": np.zeros(n), "x": np.full(n, dn / seff), "mu": np.full(n, mup), "E": np.ones(n),
+                     "E0": np.ones(n), "cell": np.ones(n, np.int32)})
+    e.transport()
+    p = e.particles()
+    e.close()
+    alive = p["E0"] >= 0
+    assert alive.all()  # every history reaches census (in the cell or a buffer)
+    cell, mu, x = p["cell"], p["mu"], p["x"]
+    cls_t = np.where(cell == 1, 2, np.where(cell == 0, 0, 1))  # near face is the left one (dn < W / 2)
+    # exit time from the distance streamed in the buffer (no collisions there)
+    dx0 = 0.6
+    left = cell == 0
+    t_exit_l = 0.5 - (dx0 - x[left]) / np.abs(mu[left])
+    lpath_t = np.log(t_exit_l * seff / lmax)
+    st = np.tile(np.array([[dn, W - dn, mup, lmax]], np.float32), (n, 1))
+    xw, cls_w, tgt_w = G.walk(4242, st)
+    for k in range(3):
+        pt, pw = np.mean(cls_t == k), np.mean(cls_w == k)
+        sd = np.sqrt(max(pt * (1 - pt), pw * (1 - pw), 1e-6) * 2.0 / n)
+        assert abs(pt - pw) < 4 * sd, (k, pt, pw)
+    mu_t, mu_w = np.abs(mu[left]), tgt_w[cls_w == 0, 1]
+    assert abs(mu_t.mean() - mu_w.mean()) < 4 * np.sqrt(mu_t.var() / len(mu_t) + mu_w.var() / len(mu_w))
+    lw = tgt_w[cls_w == 0, 0]
+    assert abs(lpath_t.mean() - lw.mean()) < 4 * np.sqrt(lpath_t.var() / len(lpath_t) + lw.var() / len(lw))
