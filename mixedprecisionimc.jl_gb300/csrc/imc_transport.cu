@@ -449,7 +449,9 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
         return true;
     };
     // one pass of the reference's while loop (src/imc_transport.jl:533-717);
-    // 0 = go on, 1 = killed or escaped, 2 = census
+    // 0 = go on, 1 = killed, 2 = census, 4 = escaped through a vacuum face.
+    // The census write and the escape tally are left to finish(), which
+    // the warp runs converged once per history.
     auto segment = [&]() -> int {
         if (++seg > cap) { flags |= (1u << 2); return 1; }
         const T dist_bx = vx > (T)0 ? m_abs((fx[xi].ws - xp) / vx) : m_abs(xp / vx);
@@ -500,15 +502,13 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
                 if (vx > (T)0) {
                     if (xi == NX - 1) {
                         if (refl_r) { vx = -vx; return 0; }
-                        flush_one<T, false>(ca.lost_acc, k, E, b_lost + s_sexp[k], flags);
-                        return 1;
+                        return 4;
                     }
                     xi += 1; xp = (T)0;
                 } else {
                     if (xi == 0) {
                         if (refl_l) { vx = -vx; return 0; }
-                        flush_one<T, false>(ca.lost_acc, k, E, b_lost + s_sexp[k], flags);
-                        return 1;
+                        return 4;
                     }
                     xi -= 1; xp = fx[xi].ws;
                 }
@@ -516,15 +516,13 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
                 if (vy > (T)0) {
                     if (yi == NY - 1) {
                         if (refl_t) { vy = -vy; return 0; }
-                        flush_one<T, false>(ca.lost_acc, k, E, b_lost + s_sexp[k], flags);
-                        return 1;
+                        return 4;
                     }
                     yi += 1; yp = (T)0;
                 } else {
                     if (yi == 0) {
                         if (refl_b) { vy = -vy; return 0; }
-                        flush_one<T, false>(ca.lost_acc, k, E, b_lost + s_sexp[k], flags);
-                        return 1;
+                        return 4;
                     }
                     yi -= 1; yp = fy[yi].ws;
                 }
@@ -538,7 +536,14 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
             if constexpr (sizeof(T) == 4) __sincosf(ang, &vy, &vx);
             else m_sincos(ang, &vy, &vx);
         }
-        if (dist == dist_cen) {
+        // census: t = 0 and the state written back by finish()
+        if (dist == dist_cen) return 2;
+        return 0;
+    };
+    auto finish = [&](int end) {
+        flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep + s_sexp[k], flags);
+        if (end == 2) {
+            // census: t = 0, write the state back (src/imc_transport.jl:700-717)
             const int cellf = xi + yi * NX;
             T Est = E;
             if (St::half) {
@@ -562,13 +567,9 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
             flush_one<T, RAD_SMT>(rad_acc, k * nc + cellf, Est, b_rad + s_sexp[k], flags);
             const int ee = exp_bound(Est) - s_sexp[k];
             emax_e = ee > emax_e ? ee : emax_e;
-            return 2;
-        }
-        return 0;
-    };
-    auto finish = [&](int end) {
-        flush_pair<T, SMT>(dep_acc, k * nc + acc_cell, acc_s, acc_c, b_dep + s_sexp[k], flags);
-        if (end == 1) {
+        } else {
+            // killed, or escaped with E through a vacuum face
+            if (end == 4) flush_one<T, false>(ca.lost_acc, k, E, b_lost + s_sexp[k], flags);
             pb.alive[i] = 0;
             ++killed;
         }
