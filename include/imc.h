@@ -369,7 +369,12 @@ int imc_surrogate_sample(const float *params, uint64_t seed, const float *state,
  * wide, a history with at least 32 mean free paths of path left before census
  * or the cut-off is moved by one network query instead of its analog
  * collisions (lmax above 1e4 is walked in 1e4 pieces); elsewhere transport
- * is analog.  ImcStepStats.surrogate_calls counts the queries. */
+ * is analog.  ImcStepStats.surrogate_calls counts the queries.  A step gate
+ * keeps the network on for the next step only when this step made at least
+ * two queries per GPU thread (2 x SMs x 1024); below that the step runs the
+ * analog transport alone.  A closed gate re-opens to measure when the step's
+ * histories have doubled since it closed and every 32 steps.  The gate reads
+ * only the step's own counts, so runs stay bit-reproducible. */
 int imc_set_surrogate(ImcHandle *h, const float *params, int64_t n_params);
 /* *active = 1 while the surrogate is on. */
 int imc_get_surrogate_active(const ImcHandle *h, int *active);
