@@ -419,16 +419,31 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
     const T dtT = (T)dtd, dsT = (T)ca.ds;
     const int ns = nsurf_slots(ca), nc = ca.nc, nslots = ca.nslots;
     const double pd = 3.141592653589793;
-    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n_new;
-         j += (long long)gridDim.x * blockDim.x) {
-        // slot = last q with slot_off[q] <= j
-        int lo = 0, hi = nslots;
-        while (hi - lo > 1) {
-            int mid = (lo + hi) >> 1;
-            if (ca.slot_off[mid] <= j) lo = mid;
-            else hi = mid;
+    // Each warp takes kEmitRun consecutive births at a time, lane l the births
+    // base + l + 32 i (every store coalesced).  A lane finds the slot of its
+    // first birth by binary search over the slot offsets (slot = last q with
+    // slot_off[q] <= j) and then walks forward for the later ones, which
+    // share its slot or sit a few slots on: one dependent search per 8
+    // births instead of one each.
+    constexpr int kEmitRun = 256;
+    const int lane = threadIdx.x & 31;
+    const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long base = wid * kEmitRun; base < n_new; base += nw * kEmitRun)
+    for (int q = -1, r = 0; r < kEmitRun; r += 32) {
+        const long long j = base + r + lane;
+        if (j >= n_new) break;
+        if (q < 0) {
+            int lo = 0, hi = nslots;
+            while (hi - lo > 1) {
+                int mid = (lo + hi) >> 1;
+                if (ca.slot_off[mid] <= j) lo = mid;
+                else hi = mid;
+            }
+            q = lo;
+        } else {
+            while (q + 1 < nslots && ca.slot_off[q + 1] <= j) ++q;
         }
-        const int q = lo;
         const long long pid = n_census + j;
         Stream rs;
         rs.init(ca.seed, step, (uint32_t)pid, kStageSource);
