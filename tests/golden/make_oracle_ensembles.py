@@ -11,12 +11,17 @@ NINPUT / NMAX scaled down (REDUCED below), 32 seeds each, FP64 particle state.
 The GPU tests (tests/test_gpu_oracle_ensembles.py) run the same reduced decks
 in every state precision and compare their ensemble means with these per cell.
 
+"c2_fp16" is the reduced slab with binary16 particle state (the oracle's
+restatement of the kernels' FP16 state): binary16 storage shifts the
+ensemble by ~0.6 sigma (mean temperature +0.18 %) against FP64 state, in the
+oracle as on the GPU, so the GPU's FP16 runs are compared with this one.
+
 The heated thick slab (tests/golden/decks/thick_heated.txt: 30 cells of 40
 mean free paths, a source in every cell, vacuum on the right) runs as
 written; its mean is the error reference of the learned surrogate's
 comparison in bench.py, where every arm reaches an error below 1 %.
 
-Run from the repository root:  python tests/golden/make_oracle_ensembles.py [c2 c3 c4 thick]
+Run from the repository root:  python tests/golden/make_oracle_ensembles.py [c2 c3 c4 thick c2_fp16]
 """
 import multiprocessing as mp
 import os
@@ -34,7 +39,10 @@ REDUCED = {
     "c3": ("c3_heatwave", {"NINPUT": "20000", "NMAX": "200000"}),
     "c4": ("c4_channel2d", {"NINPUT": "10000", "NMAX": "50000"}),
     "thick": ("thick_heated", {}),
+    "c2_fp16": ("c2_slab_fine", {"NINPUT": "20000", "NMAX": "200000"}),
 }
+# particle-state precision of each ensemble (IMC_FP64 unless listed)
+STATE = {"c2_fp16": 2}
 SEEDS = [500000 + i for i in range(32)]
 
 
@@ -56,9 +64,11 @@ def one(args):
     import mpimc
     import oracle
     inputs = reduced_inputs(name, seed)
-    inputs["PRECISION"] = np.float64
+    prec = STATE.get(name, 0)
+    if prec == 0:
+        inputs["PRECISION"] = np.float64  # FP64 state, constants in FP64
     mesh = mpimc.Mesh.mesh_generation(inputs)
-    o = oracle.Oracle(inputs, mesh)
+    o = oracle.Oracle(inputs, mesh, {"precision": prec, "scale_select_precision": prec} if prec else None)
     t0 = time.time()
     steps = o.run()
     return (o.field("temp"), o.field("radenergydens"), time.time() - t0, len(steps),
@@ -66,7 +76,7 @@ def one(args):
 
 
 def main():
-    names = [a for a in sys.argv[1:] if a in REDUCED] or [n for n in REDUCED if n != "thick"]
+    names = [a for a in sys.argv[1:] if a in REDUCED] or ["c2", "c3", "c4"]
     out = dict(np.load(OUT)) if os.path.exists(OUT) else {}
     with mp.get_context("spawn").Pool(min(8, os.cpu_count() or 1)) as pool:
         for name in names:

@@ -3,7 +3,8 @@ reduced particle counts against FP64 oracle ensembles of the same reduced decks
 (tests/golden/oracle_fp64_ensembles.npz, tests/golden/make_oracle_ensembles.py):
 per cell, the 32-seed GPU mean of the final temperature and radiation energy
 density within 3 sigma of the 32-seed oracle mean, for FP64, FP32 and FP16
-particle state (FP64 and FP32 on the 2D channel).  The mesh, physics and
+particle state (FP64 and FP32 on the 2D channel; FP16 against the oracle's
+FP16-state ensemble).  The mesh, physics and
 clock are the full configurations' -- C3 keeps its sigma = 10 T^-3 opacity
 with the TEMP_FLOOR clamp, RAMP timestepping and left surface source -- so
 these tests tie the GPU's full-size runs, whose FP64 means are the error
@@ -57,20 +58,21 @@ def test_reduced_ensemble_within_3_sigma_of_oracle(gpu_lib, name, prec):
     if not _have(name):
         pytest.skip("oracle ensemble of %s not generated" % name)
     g = np.load(GOLD)
-    n_o = len(g[name + "_seeds"])
+    # binary16 state is compared with the oracle's binary16-state ensemble:
+    # the storage shifts both alike (~0.6 sigma, mean T +0.18 % on the slab)
+    ref = name + "_fp16" if prec == "fp16" else name
+    if ref + "_temp" not in g.files:
+        pytest.skip("oracle ensemble %s not generated" % ref)
+    n_o = len(g[ref + "_seeds"])
     T, R = _ensemble(name, prec, [600000 + i for i in range(32)])
     for field, arr in (("temp", T), ("rad", R)):
-        mo, so = g["%s_%s" % (name, field)], g["%s_%s_std" % (name, field)]
+        mo, so = g["%s_%s" % (ref, field)], g["%s_%s_std" % (ref, field)]
         sg = arr.std(0, ddof=1)
         live = (so > 0) | (sg > 0)
         z = (arr.mean(0) - mo)[live] / np.sqrt(sg[live] ** 2 / len(arr) + so[live] ** 2 / n_o)
         # hundreds to thousands of cells: allow the odd 3-sigma excursion,
-        # bound the mean square and a shift of the whole profile.  Binary16
-        # state re-rounds every census energy (E/E0 to 2^-11) and position
-        # each step, noise the ensembles' own spread does not fully carry
-        # (measured on the slab: mean z^2 1.64), so its mean square is
-        # bounded at 2.0
-        z2_max = 2.0 if prec == "fp16" else 1.0 + 6.0 * np.sqrt(2.0 / live.sum()) + 0.2
+        # bound the mean square and a shift of the whole profile
+        z2_max = 1.0 + 6.0 * np.sqrt(2.0 / live.sum()) + 0.2
         assert np.mean(np.abs(z) < 3.0) >= 0.95, (field, np.sort(np.abs(z))[-8:])
         assert np.mean(z ** 2) < z2_max, (field, np.mean(z ** 2))
         assert abs(np.mean(z)) < 0.5, (field, np.mean(z))
