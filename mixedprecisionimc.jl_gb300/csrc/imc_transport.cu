@@ -284,11 +284,47 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
             do end = segment(); while (!end);
             finish(end);
         };
-        // the list (or a resume pass's queue) in chunks from the counter
-        for (long long base = warp_counter_next(&sc->work_next) * kListChunk; base < n;
-             base = warp_counter_next(&sc->work_next) * kListChunk)
-            for (int r = 0; r < kListChunk; r += 32)
-                if (base + r + lane < n) walk(base + r + lane);
+        if constexpr (!kFromQueue && !St::half) {
+            // the list in chunks from the counter; the next entry's fields
+            // are loaded while the current history walks (FP32 / FP64 state:
+            // their stored fields are the arithmetic values; measured on the
+            // 2000-cell slab, 0.496 -> 0.474 ms per launch)
+            typedef typename St::S S;
+            typedef typename St::E0S E0S;
+            uint8_t pa = 0;
+            int pcs = 0;
+            S pt = (S)0, px = (S)0, pmu = (S)0, pE = (S)0;
+            E0S pE0 = (E0S)0;
+            auto fetch = [&](long long e) {
+                pa = e < n ? pb.alive[e] : (uint8_t)0;
+                if (pa) { pcs = pb.cs[e]; pt = pb.t[e]; px = pb.x[e]; pmu = pb.ux[e]; pE = pb.E[e]; pE0 = pb.E0[e]; }
+            };
+            for (long long base = warp_counter_next(&sc->work_next) * kListChunk; base < n;
+                 base = warp_counter_next(&sc->work_next) * kListChunk) {
+                fetch(base + lane);
+                for (int r = 0; r < kListChunk; r += 32) {
+                    const long long e = base + r + lane;
+                    const bool a = pa != 0;
+                    const int ccs = pcs;
+                    t = (T)pt; x = (T)px; mu = (T)pmu; E = (T)pE; E0 = (T)pE0;
+                    if (r + 32 < kListChunk) fetch(e + 32);
+                    if (a) {
+                        i = e;
+                        cs = ccs;
+                        start(ccs);
+                        int end;
+                        do end = segment(); while (!end);
+                        finish(end);
+                    }
+                }
+            }
+        } else {
+            // the list (or a resume pass's queue) in chunks from the counter
+            for (long long base = warp_counter_next(&sc->work_next) * kListChunk; base < n;
+                 base = warp_counter_next(&sc->work_next) * kListChunk)
+                for (int r = 0; r < kListChunk; r += 32)
+                    if (base + r + lane < n) walk(base + r + lane);
+        }
     } else {
         // Long histories of unequal length: each lane starts the next history
         // as soon as its current one ends.  The warp reads the entries in
