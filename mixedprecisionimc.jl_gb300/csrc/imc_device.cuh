@@ -368,63 +368,6 @@ IMC_HD bool fix_split(double v, int b, Limbs &o) {
     return fix_place(man, e2 - b, neg, o);
 }
 
-// RN_f32(RN_f64(C * u)): the Float64 product of a Float64 constant
-// C = M * 2^eC (M its 53-bit significand) and u = m * 2^-24 (m < 2^24, the
-// 24-bit uniforms of Rand<float>), rounded to Float64 and then to Float32 --
-// the reference's `(Float32)(2pi * rand)` -- in integer arithmetic: the
-// exact 77-bit product, then the two round-to-nearest-even steps.  FP64
-// operations run at 1/64 of the FP32 rate on GB300; this takes none.
-// Results below the binary32 normal range come out as 0 (not reachable for
-// the constants used: 2 pi * 2^-24 is normal).
-IMC_HD uint64_t rne_shift(uint64_t hi, uint64_t lo, int s, uint64_t &q) {
-    // q = round-to-nearest-even of (hi:lo) / 2^s for 1 <= s <= 63; returns
-    // the carry-adjusted q (may reach 2^(bits of q) when rounding up)
-    q = (lo >> s) | (s ? (hi << (64 - s)) : 0);
-    const uint64_t rem = lo & ((1ull << s) - 1ull), half = 1ull << (s - 1);
-    if (rem > half || (rem == half && (q & 1ull))) q += 1ull;
-    return q;
-}
-IMC_HD float f32_of_f64_product(uint64_t M, int eC, uint32_t m) {
-    if (m == 0u) return 0.0f;
-    const uint64_t A = (uint64_t)m * (M & 0xFFFFFFFFull);  // < 2^56
-    const uint64_t B = (uint64_t)m * (M >> 32);            // < 2^45
-    const uint64_t lo = A + (B << 32);
-    const uint64_t hi = (B >> 32) + (lo < A ? 1ull : 0ull);
-    const int L = hi ? 64 + bitlen64(hi) : bitlen64(lo);
-    int e = eC - 24;
-    uint64_t q = lo;  // the Float64 product's significand: q * 2^e
-    if (L > 53) {
-        const int s = L - 53;
-        rne_shift(hi, lo, s, q);
-        e += s;
-        if (q >> 53) { q >>= 1; e += 1; }
-    }
-    const int Lq = bitlen64(q);
-    uint64_t f = q;  // the Float32 result's significand: f * 2^e
-    if (Lq > 24) {
-        const int s = Lq - 24;
-        rne_shift(0ull, q, s, f);
-        e += s;
-        if (f >> 24) { f >>= 1; e += 1; }
-    }
-    // normalise f to 24 bits and assemble the binary32 bits
-    const int Lf = bitlen64(f);
-    f <<= (24 - Lf);
-    e -= (24 - Lf);
-    const int be = e + 23 + 127;
-    if (be <= 0) return 0.0f;
-    if (be >= 255) return INFINITY;
-    const uint32_t bits = ((uint32_t)be << 23) | ((uint32_t)f & 0x7FFFFFu);
-#ifdef __CUDA_ARCH__
-    return __uint_as_float(bits);
-#else
-    float r; memcpy(&r, &bits, 4); return r;
-#endif
-}
-// significand and exponent of Float64(2 pi) = 0x401921FB54442D18
-constexpr uint64_t kTwoPiM = 0x1921FB54442D18ull;
-constexpr int kTwoPiE = 2 - 52;
-
 // Energy scales and the tally exponents.  A particle of scale k carries
 // E = e_true * scale_k; each tally slot of scale k holds its values times
 // 2^-scale_exp(scale_k), i.e. within a factor two of true energies, so one

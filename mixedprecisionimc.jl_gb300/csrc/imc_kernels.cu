@@ -491,14 +491,8 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
                     xpos = (sizeof(T) == 4 ? (T)ca.dxf[ix] : (T)ca.dx[ix]) * Rand<T>::u(rs) * dsT;
                     ypos = face == 0 ? (T)(0.001 * (double)(T)ca.dy[0] * (double)dsT)
                                      : (T)(0.999 * (double)(T)ca.dy[ny - 1] * (double)dsT);
-                    if constexpr (sizeof(T) == 4) {
-                        // -pi u in Float64, rounded to binary32 (integer form, f32_of_f64_product)
-                        const uint32_t m = rs.next() >> 8;
-                        ang = face == 0 ? (T)((T)pd * ((float)m * 0x1p-24f)) : -f32_of_f64_product(kTwoPiM, kTwoPiE - 1, m);
-                    } else {
-                        T u = Rand<T>::u(rs);
-                        ang = face == 0 ? (T)((T)pd * u) : (T)(-pd * (double)u);
-                    }
+                    T u = Rand<T>::u(rs);
+                    ang = face == 0 ? (T)((T)pd * u) : (T)(-pd * (double)u);
                 } else {
                     iy = idx;
                     ix = face == 2 ? 0 : nx - 1;
@@ -507,33 +501,19 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
                     // the reference scales y by mesh.dx[j] (src/imc_sourcing.jl:301,316)
                     const double wq = iy < nx ? ca.dx[iy] : ca.dy[iy];
                     ypos = (T)wq * Rand<T>::u(rs) * dsT;
-                    if constexpr (sizeof(T) == 4) {
-                        // pi (0.5 -+ u) in Float64: (0.5 -+ u) = (2^23 -+ m) 2^-24 exactly
-                        const uint32_t m = rs.next() >> 8;
-                        const uint32_t h23 = 1u << 23;
-                        if (face == 2) ang = m <= h23 ? f32_of_f64_product(kTwoPiM, kTwoPiE - 1, h23 - m)
-                                                      : -f32_of_f64_product(kTwoPiM, kTwoPiE - 1, m - h23);
-                        else ang = f32_of_f64_product(kTwoPiM, kTwoPiE - 1, h23 + m);
-                    } else {
-                        T u = Rand<T>::u(rs);
-                        ang = face == 2 ? (T)(pd * (0.5 - (double)u)) : (T)(pd * (0.5 + (double)u));
-                    }
+                    T u = Rand<T>::u(rs);
+                    ang = face == 2 ? (T)(pd * (0.5 - (double)u)) : (T)(pd * (0.5 + (double)u));
                 }
             } else {
                 // body / source births (src/imc_sourcing.jl:326-366)
                 const int cell = q < ns + nc ? q - ns : q - ns - nc;
                 ix = cell % ca.nx;
                 iy = cell / ca.nx;
-                if constexpr (sizeof(T) == 4) {
-                    // the widths and 2 pi u in Float64 rounded to binary32, without FP64 operations
-                    xpos = (T)ca.dxf[ix] * Rand<T>::u(rs) * dsT;
-                    ypos = (T)ca.dyf[iy] * Rand<T>::u(rs) * dsT;
-                    ang = f32_of_f64_product(kTwoPiM, kTwoPiE, rs.next() >> 8);
-                } else {
-                    xpos = (T)ca.dx[ix] * Rand<T>::u(rs) * dsT;
-                    ypos = (T)ca.dy[iy] * Rand<T>::u(rs) * dsT;
-                    ang = (T)(2.0 * pd * (double)Rand<T>::u(rs));
-                }
+                // binary32 widths precomputed (no per-birth conversion); the
+                // angle is the reference's Float64 2 pi rand rounded to T
+                xpos = (sizeof(T) == 4 ? (T)ca.dxf[ix] : (T)ca.dx[ix]) * Rand<T>::u(rs) * dsT;
+                ypos = (sizeof(T) == 4 ? (T)ca.dyf[iy] : (T)ca.dy[iy]) * Rand<T>::u(rs) * dsT;
+                ang = (T)(2.0 * pd * (double)Rand<T>::u(rs));
                 st = dtT * Rand<T>::u(rs);
             }
             T ux, uy;

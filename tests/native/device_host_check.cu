@@ -6,10 +6,6 @@
 //   F b v1 v2 ... (until '.')    -> exact fixed-point total of the values, as
 //                                   signed limb sums "a0 a1 a2" and the double
 //   R prec n v1..vn K s1..sK     -> sorter<prec> product (hex) and scale index
-//   A M eC m1 m2 ... (until '.') -> per 24-bit m: f32_of_f64_product(M, eC, m) as hex bits
-//   X M eC                       -> over every m < 2^24: the number of m where
-//                                   f32_of_f64_product differs from the host's
-//                                   (float)((double)C * (double)(m * 2^-24))
 //   W b v1 v2 ... (until '.')    -> per FP32 value: "1 l0 l1 l2" from f32_words
 //                                   (words as the signed limbs of fix_split),
 //                                   "0" where f32_words declines, and
@@ -54,25 +50,6 @@ int main() {
                 acc[0] += L.l0; acc[1] += L.l1; acc[2] += L.l2;
             }
             printf("%d %lld %lld %lld %.17g\n", ok ? 1 : 0, acc[0], acc[1], acc[2], fix_value(acc, b));
-        } else if (cmd == "A") {
-            unsigned long long M; int eC; in >> M >> eC;
-            std::string tok;
-            while (in >> tok && tok != ".") {
-                const uint32_t m = (uint32_t)strtoul(tok.c_str(), nullptr, 10);
-                const float r = f32_of_f64_product(M, eC, m);
-                uint32_t b; memcpy(&b, &r, 4);
-                printf("%08x\n", b);
-            }
-        } else if (cmd == "X") {
-            unsigned long long M; int eC; in >> M >> eC;
-            const double C = std::ldexp((double)M, eC);
-            long long bad = 0;
-            for (uint32_t m = 0; m < (1u << 24); ++m) {
-                const float want = (float)(C * (double)((float)m * 0x1p-24f));
-                const float got = f32_of_f64_product(M, eC, m);
-                if (std::memcmp(&want, &got, 4) != 0) ++bad;
-            }
-            printf("%lld\n", bad);
         } else if (cmd == "W") {
             int b; in >> b;
             std::string tok;

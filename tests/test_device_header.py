@@ -148,26 +148,3 @@ def test_f32_two_word_placement_equals_fix_split(tool):
                 assert e - 23 - b < 0, (b, v, line)
     assert took > 300
 
-
-def test_f32_of_f64_product_is_the_double_rounding(tool):
-    """The integer form of Float32(Float64(C) * u) used for the 2D birth angle
-    (C = 2 pi) equals numpy's float64 product rounded to float32, including the
-    ties that double rounding creates, for every kind of 24-bit m."""
-    rng = np.random.default_rng(7)
-    ms = list(rng.integers(0, 1 << 24, 3000)) + [0, 1, 2, 3, (1 << 24) - 1, 1 << 23, (1 << 23) + 1, 12345]
-    two_pi = 6.283185307179586
-    M = 0x1921FB54442D18
-    assert float(M) * 2.0 ** (2 - 52) == two_pi
-    for C, Mc, eC in ((two_pi, M, 2 - 52), (0.01, 0x147AE147AE147B, -7 - 52), (1.0 / 3.0, 0x15555555555555, -2 - 52)):
-        assert float(Mc) * 2.0 ** eC == C
-        out = tool(["A %d %d %s ." % (Mc, eC, " ".join(str(int(m)) for m in ms))])
-        for m, h in zip(ms, out):
-            want = np.float32(np.float64(C) * np.float64(np.float32(int(m) * 2.0 ** -24)))
-            assert int(h, 16) == int(want.view(np.uint32)), (C, m, h, want)
-
-
-def test_f32_of_f64_product_exhaustive_for_two_pi(tool):
-    """Every one of the 2^24 uniforms: the integer double rounding equals the
-    host's IEEE Float64 product converted to Float32 (C = 2 pi and 0.01)."""
-    assert tool(["X %d %d" % (0x1921FB54442D18, 2 - 52)]) == ["0"]
-    assert tool(["X %d %d" % (0x147AE147AE147B, -7 - 52)]) == ["0"]
