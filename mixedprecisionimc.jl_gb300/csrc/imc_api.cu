@@ -347,11 +347,10 @@ int enqueue_step(ImcHandle *h, bool with_events, int ev_slot) {
     if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot], st));
     run_transport(h, bufs, st);
     if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot + 1], st));
-    // finalize + tally, then the compaction (it touches no cell field), then
-    // energycheck + timestep: the reference's order in four launches
-    launch_finalize_tally(h->ca, h->d_sc, st);
+    // the compaction (it reads no cell field and the tally no particle), then
+    // finalize + tally + energycheck + timestep in one launch
     launch_compact(h->ca, h->d_sc, h->prec, bufs, h->tile_cnt, h->tile_off, h->ntiles_cap, false, st);
-    launch_energycheck_timestep(h->ca, h->d_sc, h->d_stats, h->stats_cap, st);
+    launch_tally_check_timestep(h->ca, h->d_sc, h->d_stats, h->stats_cap, st);
     CKL(h);
     return IMC_OK;
 }
@@ -1282,10 +1281,10 @@ int imc_get_surrogate_active(const ImcHandle *h, int *active) {
 
 int imc_kernels_per_step(const ImcHandle *h, int *count) {
     if (!h || !count) return IMC_ERR_INVALID_ARG;
-    // update, source x5, transport, finalize + tally, compact x4,
+    // update, source x5, transport, compact x4, finalize + tally +
     // energycheck + timestep; the surrogate transport is 1 + 2 kSurrRounds
     // kernels
-    *count = 13 + (h->ca.surr_image ? 2 * kSurrRounds : 0);
+    *count = 12 + (h->ca.surr_image ? 2 * kSurrRounds : 0);
     return IMC_OK;
 }
 

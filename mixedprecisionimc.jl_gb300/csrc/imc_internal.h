@@ -56,6 +56,7 @@ struct Scalars {
     int compact_now;                   // this step compacts the list
     int surr_gate;                     // learned surrogate: this step may set histories aside
     long long surr_closed_h;           // histories of the step that last closed the gate
+    unsigned int tally_blocks_done;    // fused tally + energy check: blocks finished (the last one checks)
 };
 
 struct CellArgs {
@@ -171,6 +172,9 @@ void launch_energycheck(const CellArgs &ca, Scalars *sc, DevStats *stats, long l
 void launch_timestep(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 // the step sequence's fused launches: finalize + tally, energycheck + timestep
 void launch_finalize_tally(const CellArgs &ca, Scalars *sc, cudaStream_t st);
+// finalize + tally + energycheck + timestep in one launch (the step sequence)
+void launch_tally_check_timestep(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap,
+                                 cudaStream_t st);
 void launch_energycheck_timestep(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap,
                                  cudaStream_t st);
 void launch_prepare_transport(const CellArgs &ca, Scalars *sc, cudaStream_t st);

@@ -870,18 +870,12 @@ __device__ __forceinline__ void advance_clock(const CellArgs &ca, Scalars *sc) {
     sc->step += 1u;
 }
 
-// EnergyCheck.energychecker (src/imc_energycheck.jl:19-38).  One warp per
-// partial-sum group (K deposition scales, then the radiation energy).
-template <bool STEP>
-__global__ void __launch_bounds__(544) k_energycheck(CellArgs ca, Scalars *sc, DevStats *stats, long long stats_cap) {
-    __shared__ double g[17];
-    const int warp = threadIdx.x >> 5, np = ca.K + 1;
-    if (warp < np) {
-        double v = warp_sum_partials(ca.part_tally, ca.nblk_cell, np, warp);
-        if ((threadIdx.x & 31) == 0) g[warp] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x != 0) return;
+// EnergyCheck.energychecker (src/imc_energycheck.jl:19-38) from the sums of
+// the tally's per-block partials (g[k]: deposited energy of scale k, g[K]:
+// radiation energy), by one thread: the balance, the step's statistics, the
+// learned surrogate's gate, and with STEP the clock.
+__device__ void energycheck_done(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap,
+                                 const double *g, bool step) {
     double totdep = 0.0;
     for (int k = 0; k < ca.K; ++k) totdep += g[k];
     const double radenergy = g[ca.K];
@@ -928,7 +922,51 @@ __global__ void __launch_bounds__(544) k_energycheck(CellArgs ca, Scalars *sc, D
         }
         if ((sc->step + 1u) % kSurrProbe == 0u) sc->surr_gate = 1;
     }
-    if (STEP) advance_clock(ca, sc);  // the step sequence: timestep in the same launch
+    if (step) advance_clock(ca, sc);  // the step sequence: timestep in the same launch
+}
+
+// EnergyCheck.energychecker as its own launch: one warp per partial-sum
+// group (K deposition scales, then the radiation energy).
+template <bool STEP>
+__global__ void __launch_bounds__(544) k_energycheck(CellArgs ca, Scalars *sc, DevStats *stats, long long stats_cap) {
+    __shared__ double g[17];
+    const int warp = threadIdx.x >> 5, np = ca.K + 1;
+    if (warp < np) {
+        double v = warp_sum_partials(ca.part_tally, ca.nblk_cell, np, warp);
+        if ((threadIdx.x & 31) == 0) g[warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) energycheck_done(ca, sc, stats, stats_cap, g, STEP);
+}
+
+// Finalize + tally per cell, then, in the block that finishes last, the
+// energy check and the timestep: one launch for the step's tail.  Each
+// block publishes its partial sums before taking a ticket; the last block
+// sums every block's partials in block order (the same fixed order as
+// k_energycheck, so the same values).
+__global__ void __launch_bounds__(kCellThreads) k_tally_check(CellArgs ca, Scalars *sc, DevStats *stats,
+                                                             long long stats_cap) {
+    static_assert(kCellThreads == 32, "one-warp blocks");
+    __shared__ DD sh[kCellThreads];
+    __shared__ double g[17];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    finalize_cell(ca, sc, i);
+    tally_cell(ca, sc, i, sh);
+    __threadfence();
+    unsigned ticket = 0;
+    if (threadIdx.x == 0) ticket = atomicAdd(&sc->tally_blocks_done, 1u);
+    ticket = __shfl_sync(0xFFFFFFFFu, ticket, 0);
+    if (ticket != gridDim.x - 1u) return;
+    __threadfence();
+    const int np = ca.K + 1;
+    for (int q = 0; q < np; ++q) {
+        const double v = warp_sum_partials(ca.part_tally, ca.nblk_cell, np, q);
+        if (threadIdx.x == 0) g[q] = v;
+    }
+    if (threadIdx.x == 0) {
+        sc->tally_blocks_done = 0u;
+        energycheck_done(ca, sc, stats, stats_cap, g, true);
+    }
 }
 
 __global__ void k_timestep(CellArgs ca, Scalars *sc) { advance_clock(ca, sc); }
@@ -937,6 +975,11 @@ void launch_timestep(const CellArgs &ca, Scalars *sc, cudaStream_t st) { k_times
 
 void launch_energycheck(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap, cudaStream_t st) {
     k_energycheck<false><<<1, 32 * (ca.K + 1), 0, st>>>(ca, sc, stats, stats_cap);
+}
+
+void launch_tally_check_timestep(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap,
+                                 cudaStream_t st) {
+    k_tally_check<<<ca.nblk_cell, kCellThreads, 0, st>>>(ca, sc, stats, stats_cap);
 }
 
 void launch_energycheck_timestep(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap,
