@@ -422,9 +422,10 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
     // Each warp takes kEmitRun consecutive births at a time, lane l the births
     // base + l + 32 i (every store coalesced).  A lane finds the slot of its
     // first birth by binary search over the slot offsets (slot = last q with
-    // slot_off[q] <= j) and then walks forward for the later ones, which
-    // share its slot or sit a few slots on: one dependent search per 8
-    // births instead of one each.
+    // slot_off[q] <= j) and the later ones by galloping forward from there
+    // (q + 1, q + 2, q + 4, ... then bisection): one or two loads where the
+    // slot holds many births (the channel's surface segment), a few where
+    // it holds a handful (the CELLMIN births of every body cell).
     constexpr int kEmitRun = 256;
     const int lane = threadIdx.x & 31;
     const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -441,8 +442,20 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
                 else hi = mid;
             }
             q = lo;
-        } else {
-            while (q + 1 < nslots && ca.slot_off[q + 1] <= j) ++q;
+        } else if (q + 1 < nslots && ca.slot_off[q + 1] <= j) {
+            int lo = q + 1, step = 2, hi = q + 2;  // slot_off[lo] <= j
+            while (hi < nslots && ca.slot_off[hi] <= j) {
+                lo = hi;
+                step <<= 1;
+                hi = q + step;
+            }
+            if (hi > nslots) hi = nslots;  // slot_off[hi] > j, or hi == nslots
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (ca.slot_off[mid] <= j) lo = mid;
+                else hi = mid;
+            }
+            q = lo;
         }
         const long long pid = n_census + j;
         Stream rs;
