@@ -397,11 +397,13 @@ def c4_section(n32=2, n64=2):
 
 
 def c5_section(n_err=16):
-    """The batched ensemble (256 1D decks of tests/golden/c5_decks.py) run
-    side by side with imc_run_batch: learned surrogate + FP32 state and plain
-    FP32 state over all 256 decks (throughput), and per-deck temperature error
-    on the first n_err decks: learned+FP32 and plain FP64 runs (seeds + 1000)
-    against plain FP64 runs of other seeds (seeds + 2000)."""
+    """The batched ensemble (256 1D decks of tests/golden/c5_decks.py): run
+    side by side with imc_run_batch (learned surrogate + FP32 state, plain
+    FP32 state) and stepped together with imc_run_batch_fused (plain FP32, one
+    transport launch per step over all 256 decks, checked bit-identical to the
+    side-by-side run) over all 256 decks (throughput), and per-deck
+    temperature error on the first n_err decks: learned+FP32 and plain FP64
+    runs (seeds + 1000) against plain FP64 runs of other seeds (seeds + 2000)."""
     import numpy as np
     import mpimc
     from mpimc import surrogate
@@ -410,13 +412,13 @@ def c5_section(n_err=16):
 
     P = surrogate.train()
 
-    def batch(n, seed_offset, overrides=None, params=None):
+    def batch(n, seed_offset, overrides=None, params=None, fused=False):
         engines = [mpimc.Engine(i, m, overrides) for i, m in c5_decks(n, seed_offset=seed_offset)]
         try:
             if params is not None:
                 for e in engines:
                     e.set_surrogate(params)
-            steps, wall = mpimc.run_batch(engines, threads=32)
+            steps, wall = mpimc.run_batch(engines, threads=32, fused=fused)
             tot = np.array([e.totals() for e in engines], dtype=np.float64)
             temps = [e.field("temp") for e in engines]
         finally:
@@ -428,6 +430,8 @@ def c5_section(n_err=16):
     fp64 = {"precision": 0, "scale_select_precision": 0}
     learned = batch(256, 0, None, P)
     plain = batch(256, 0)
+    fused = batch(256, 0, fused=True)
+    same = all(np.array_equal(a, b) for a, b in zip(plain["temp"], fused["temp"]))
     ref = batch(n_err, 2000, fp64)
     l_err = batch(n_err, 1000, None, P)
     f_err = batch(n_err, 1000, fp64)
@@ -450,6 +454,9 @@ def c5_section(n_err=16):
                              "surrogate_calls": learned["surrogate_calls"], "segments": learned["segments"]},
             "fp32": {"wall_s": plain["wall_s"], "segments_per_s": plain["segments"] / plain["wall_s"],
                      "histories_per_s": plain["histories"] / plain["wall_s"], "segments": plain["segments"]},
+            "fp32_fused": {"wall_s": fused["wall_s"], "segments_per_s": fused["segments"] / fused["wall_s"],
+                           "histories_per_s": fused["histories"] / fused["wall_s"], "segments": fused["segments"],
+                           "identical_to_side_by_side": bool(same and fused["segments"] == plain["segments"])},
             "error_decks": n_err,
             "relerr_T_learned_fp32": {"rms": rms_l, "median": float(np.median(rl)), "max": float(np.max(rl)),
                                       "wall_s": l_err["wall_s"]},

@@ -228,6 +228,21 @@ int imc_run(ImcHandle *h, int64_t max_steps, ImcStepStats *stats,
  * first handle that failed, whose index goes to *failed (-1 if none). */
 int imc_run_batch(ImcHandle *const *hs, int32_t n, int64_t max_steps, int32_t n_threads, int64_t *steps,
                   double *wall_ms, int32_t *failed);
+/* Batched ensemble with one transport launch per step over every deck: each
+ * step is one CUDA graph -- every deck's update + sourcing, then a single
+ * persistent transport kernel whose blocks take work chunks from each deck's
+ * list in turn (with that deck's cell table and private tallies), then every
+ * deck's compaction and tally + energycheck + timestep.  Each deck's result
+ * is bit-identical to imc_run's.  The decks step together; a deck whose clock
+ * ends leaves the group.  Requires every handle 1D, on one device, of one
+ * state precision, without the surrogate, and with its tallies in shared
+ * memory (up to ~4100 cells for FP32 state with one energy scale), at most 256 decks; otherwise
+ * IMC_ERR_INVALID_ARG with *failed = the first handle that does not qualify.
+ * Arguments and results as imc_run_batch; the batch stops at the first deck
+ * that raises an error flag.  No counterpart in the reference (a loop over
+ * its decks is the user's). */
+int imc_run_batch_fused(ImcHandle *const *hs, int32_t n, int64_t max_steps, int64_t *steps, double *wall_ms,
+                        int32_t *failed);
 
 /* Checkpoint / resume.  imc_save_state copies the whole simulation state --
  * clock, device scalars (energy balance, fixed-point ranges), cell fields and

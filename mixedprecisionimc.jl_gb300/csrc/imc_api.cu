@@ -337,20 +337,27 @@ void run_transport(ImcHandle *h, PBufPair bufs, cudaStream_t st) {
     else launch_transport(h->ca, h->d_sc, h->prec, bufs, h->grid_transport, st);
 }
 
-// the kernel sequence of one step, asynchronous on h->stream; the list's
-// buffer is chosen on the device, so the same sequence serves every step
-int enqueue_step(ImcHandle *h, bool with_events, int ev_slot) {
-    const PBufPair bufs = pair(h);
-    cudaStream_t st = h->stream;
+// The kernel sequence of one step, asynchronous on `st`; the list's buffer is
+// chosen on the device, so the same sequence serves every step.  Its halves
+// around the transport: update + sourcing, then the compaction (it reads no
+// cell field and the tally no particle) and finalize + tally + energycheck +
+// timestep in one launch.
+void enqueue_before_transport(ImcHandle *h, cudaStream_t st) {
     launch_update(h->ca, h->d_sc, st);
-    launch_source(h->ca, h->d_sc, h->prec, bufs, h->grid_emit, st);
-    if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot], st));
-    run_transport(h, bufs, st);
-    if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot + 1], st));
-    // the compaction (it reads no cell field and the tally no particle), then
-    // finalize + tally + energycheck + timestep in one launch
-    launch_compact(h->ca, h->d_sc, h->prec, bufs, h->tile_cnt, h->tile_off, h->ntiles_cap, false, st);
+    launch_source(h->ca, h->d_sc, h->prec, pair(h), h->grid_emit, st);
+}
+void enqueue_after_transport(ImcHandle *h, cudaStream_t st) {
+    launch_compact(h->ca, h->d_sc, h->prec, pair(h), h->tile_cnt, h->tile_off, h->ntiles_cap, false, st);
     launch_tally_check_timestep(h->ca, h->d_sc, h->d_stats, h->stats_cap, st);
+}
+
+int enqueue_step(ImcHandle *h, bool with_events, int ev_slot) {
+    cudaStream_t st = h->stream;
+    enqueue_before_transport(h, st);
+    if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot], st));
+    run_transport(h, pair(h), st);
+    if (with_events) CK(h, cudaEventRecord(h->ev_pool[2 * ev_slot + 1], st));
+    enqueue_after_transport(h, st);
     CKL(h);
     return IMC_OK;
 }
@@ -452,6 +459,164 @@ int check_device(ImcHandle *h, int *dev, int *sms) {
     if (!(p.major == 10 && p.minor == 3))
         return fail(h, IMC_ERR_NO_DEVICE, std::string("libimc is built for sm_103a; device is ") + p.name);
     *sms = p.multiProcessorCount;
+    return IMC_OK;
+}
+
+// ------------------------------------------------------------- fused batch
+// One half of a handle's step sequence (before or after the transport),
+// captured as a graph.
+int capture_half(ImcHandle *h, bool before, cudaGraph_t *g) {
+    std::lock_guard<std::mutex> lock(g_capture_mutex);
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    if (before) enqueue_before_transport(h, h->stream);
+    else enqueue_after_transport(h, h->stream);
+    const cudaError_t le = cudaGetLastError();
+    const cudaError_t e = cudaStreamEndCapture(h->stream, g);
+    if (e != cudaSuccess) return fail(h, IMC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    if (le != cudaSuccess) {
+        cudaGraphDestroy(*g);
+        return fail(h, IMC_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(le));
+    }
+    return IMC_OK;
+}
+
+// The fused batch's step graph.
+struct FusedBatch {
+    cudaStream_t st = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<int> members;    // deck indices of the graph, in launch order
+    ~FusedBatch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (st) cudaStreamDestroy(st);
+    }
+    void drop() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+    }
+};
+// the fused transport's deck arguments live in one constant-memory table:
+// one fused batch at a time in the process
+std::mutex g_fused_mutex;
+
+Deck1DArgs deck1d_args(const CellArgs &ca) {
+    Deck1DArgs a{};
+    a.nx = ca.nx; a.nc = ca.nc; a.K = ca.K;
+    a.bc[0] = ca.bc[0]; a.bc[1] = ca.bc[1];
+    a.dx = ca.dx; a.sa = ca.sa; a.fleck = ca.fleck; a.ss = ca.ss; a.scales = ca.scales;
+    a.dep_acc = ca.dep_acc; a.rad_acc = ca.rad_acc; a.lost_acc = ca.lost_acc;
+    a.c = ca.c; a.ds = ca.ds;
+    a.seg_cap = ca.seg_cap;
+    a.seed = ca.seed;
+    return a;
+}
+
+PBufPair1D pair1d(const ImcHandle *h) {
+    PBufPair1D p{};
+    for (int b = 0; b < 2; ++b) {
+        const PBufRaw &r = h->buf[b];
+        p.b[b].t = r.t; p.b[b].x = r.x; p.b[b].ux = r.ux; p.b[b].E = r.E; p.b[b].E0 = r.E0;
+        p.b[b].cs = r.cs; p.b[b].alive = r.alive;
+    }
+    return p;
+}
+
+// Builds the step graph over `members`: every deck's update + sourcing, one
+// fused transport launch over all of them, then every deck's compaction and
+// tally + energycheck + timestep.  *bad: the deck whose capture failed.
+int build_fused(FusedBatch &F, ImcHandle *const *hs, const std::vector<int> &members, int prec, int *bad) {
+    F.drop();
+    F.members.clear();
+    const int n = (int)members.size();
+    ImcHandle *h0 = hs[members[0]];
+    std::vector<Deck1DArgs> cas((size_t)n);
+    std::vector<PBufPair1D> bufs((size_t)n);
+    std::vector<Scalars *> scs((size_t)n);
+    int smem = 0;
+    for (int j = 0; j < n; ++j) {
+        ImcHandle *h = hs[members[j]];
+        cas[j] = deck1d_args(h->ca);
+        bufs[j] = pair1d(h);
+        scs[j] = h->d_sc;
+        smem = std::max(smem, transport_shape(h->ca, prec).smem);
+    }
+    CK(h0, set_transport_multi_decks(cas.data(), bufs.data(), scs.data(), n, F.st));
+    const void *kp = transport_multi_ptr(prec);
+    const int block = transport_multi_block(prec);
+    CK(h0, raise_smem_limit(kp, smem));
+    int per_sm = 0;
+    CK(h0, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp, block, smem));
+    if (per_sm < 1) return fail(h0, IMC_ERR_CUDA, "fused transport: no block fits on an SM");
+    const int grid = per_sm * h0->sm_count;
+    cudaGraph_t G = nullptr;
+    CK(h0, cudaGraphCreate(&G, 0));
+    int rc = IMC_OK;
+    std::vector<cudaGraphNode_t> before((size_t)n);
+    cudaGraphNode_t tn = nullptr;
+    auto add_half = [&](int j, bool first, const cudaGraphNode_t *deps, size_t ndeps, cudaGraphNode_t *node) {
+        ImcHandle *h = hs[members[j]];
+        cudaGraph_t g = nullptr;
+        if ((rc = capture_half(h, first, &g))) { *bad = members[j]; return; }
+        const cudaError_t e = cudaGraphAddChildGraphNode(node, G, deps, ndeps, g);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            rc = fail(h, IMC_ERR_CUDA, std::string("child graph: ") + cudaGetErrorString(e));
+            *bad = members[j];
+        }
+    };
+    for (int j = 0; j < n && !rc; ++j) add_half(j, true, nullptr, 0, &before[j]);
+    if (!rc) {
+        int nd = n;
+        void *args[] = {&nd};
+        cudaKernelNodeParams p{};
+        p.func = const_cast<void *>(kp);
+        p.gridDim = dim3((unsigned)grid);
+        p.blockDim = dim3((unsigned)block);
+        p.sharedMemBytes = (unsigned)smem;
+        p.kernelParams = args;
+        p.extra = nullptr;
+        const cudaError_t e = cudaGraphAddKernelNode(&tn, G, before.data(), (size_t)n, &p);
+        if (e != cudaSuccess) rc = fail(h0, IMC_ERR_CUDA, std::string("fused transport node: ") + cudaGetErrorString(e));
+    }
+    for (int j = 0; j < n && !rc; ++j) {
+        cudaGraphNode_t after = nullptr;
+        add_half(j, false, &tn, 1, &after);
+    }
+    if (!rc) {
+        const cudaError_t e = cudaGraphInstantiate(&F.exec, G, 0);
+        if (e != cudaSuccess) {
+            F.exec = nullptr;
+            rc = fail(h0, IMC_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        }
+    }
+    cudaGraphDestroy(G);
+    if (!rc) F.members = members;
+    return rc;
+}
+
+// The host clock mirror and the totals after `done` steps run on the device,
+// whose statistics start at ring slot `slot0` (copied in at most two pieces).
+int absorb_steps(ImcHandle *h, unsigned long long slot0, int64_t done, ImcStepStats *stats, unsigned *allflags) {
+    std::vector<DevStats> ds((size_t)done);
+    const unsigned long long cap = (unsigned long long)h->stats_cap;
+    for (int64_t s = 0; s < done;) {
+        const unsigned long long slot = (slot0 + (unsigned long long)s) % cap;
+        const int64_t len = std::min<int64_t>(done - s, (int64_t)(cap - slot));
+        CK(h, hcopy(h, &ds[(size_t)s], h->d_stats + slot, sizeof(DevStats) * (size_t)len, cudaMemcpyDeviceToHost));
+        s += len;
+    }
+    for (int64_t s = 0; s < done; ++s) {
+        if (stats) to_stats(ds[s], &stats[s]);
+        *allflags |= ds[s].error_flags;
+        h->tot_segments += ds[s].segments;
+        h->tot_histories += ds[s].n_census_in + ds[s].n_sourced;
+        h->tot_calls += ds[s].surrogate_calls;
+        bool fin;
+        host_timestep(h->deck, h->t, h->dt, fin);
+        h->finished = fin;
+        h->step += 1;
+    }
+    if (done > 0) to_stats(ds[done - 1], &h->last);
+    h->stage = Stage::Fresh;
     return IMC_OK;
 }
 
@@ -823,26 +988,8 @@ int imc_run(ImcHandle *h, int64_t max_steps, ImcStepStats *stats, int64_t *n_ste
     float ms = 0.f;
     CK(h, cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
     if (device_ms) *device_ms = ms;
-    // host clock mirror and statistics
-    std::vector<DevStats> ds((size_t)done_steps);
-    for (int64_t s = 0; s < done_steps; ++s) {
-        unsigned long long slot = (slot0 + (unsigned long long)s) % (unsigned long long)h->stats_cap;
-        CK(h, hcopy(h, &ds[s], h->d_stats + slot, sizeof(DevStats), cudaMemcpyDeviceToHost));
-    }
     unsigned allflags = 0;
-    for (int64_t s = 0; s < done_steps; ++s) {
-        if (stats) to_stats(ds[s], &stats[s]);
-        allflags |= ds[s].error_flags;
-        h->tot_segments += ds[s].segments;
-        h->tot_histories += ds[s].n_census_in + ds[s].n_sourced;
-        h->tot_calls += ds[s].surrogate_calls;
-        bool fin;
-        host_timestep(h->deck, h->t, h->dt, fin);
-        h->finished = fin;
-        h->step += 1;
-    }
-    if (done_steps > 0) to_stats(ds[done_steps - 1], &h->last);
-    h->stage = Stage::Fresh;
+    if ((rc = absorb_steps(h, slot0, done_steps, stats, &allflags))) return rc;
     if (n_steps) *n_steps = done_steps;
     return flags_status(h, allflags);
 }
@@ -884,6 +1031,132 @@ int imc_run_batch(ImcHandle *const *hs, int32_t n, int64_t max_steps, int32_t n_
     if (wall_ms) *wall_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
     if (failed) *failed = first_bad.load();
     return first_rc.load();
+}
+
+int imc_run_batch_fused(ImcHandle *const *hs, int32_t n, int64_t max_steps, int64_t *steps, double *wall_ms,
+                        int32_t *failed) {
+    if (!hs || n < 1 || n > kFusedMaxDecks) return IMC_ERR_INVALID_ARG;
+    for (int32_t i = 0; i < n; ++i)
+        if (!hs[i]) return IMC_ERR_INVALID_ARG;
+    for (int32_t i = 0; i < n; ++i)
+        for (int32_t j = 0; j < i; ++j)
+            if (hs[i] == hs[j]) return IMC_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> fused_lock(g_fused_mutex);
+    if (failed) *failed = -1;
+    if (steps)
+        for (int32_t i = 0; i < n; ++i) steps[i] = 0;
+    if (wall_ms) *wall_ms = 0.0;
+    const int prec = hs[0]->prec, dev = hs[0]->device;
+    for (int32_t i = 0; i < n; ++i) {
+        ImcHandle *h = hs[i];
+        if (h->device != dev || h->geometry != 1 || h->prec != prec || h->ca.surr_image ||
+            !transport_shape(h->ca, prec).smem_tally) {
+            if (failed) *failed = i;
+            return fail(h, IMC_ERR_INVALID_ARG,
+                        "fused batch: every deck 1D, on one device, of one state precision, without the "
+                        "surrogate, with its tallies in shared memory");
+        }
+    }
+    if (cudaSetDevice(dev) != cudaSuccess) return fail(hs[0], IMC_ERR_CUDA, "cudaSetDevice");
+    const auto t0 = std::chrono::steady_clock::now();
+    // steps of each deck from the host clock mirrors, as imc_run counts them
+    std::vector<int64_t> N((size_t)n, 0), done((size_t)n, 0);
+    std::vector<unsigned long long> slot0((size_t)n, 0);
+    std::vector<long long> ncen((size_t)n, 0);
+    int rc = IMC_OK, bad = -1;
+    for (int32_t i = 0; i < n && !rc; ++i) {
+        ImcHandle *h = hs[i];
+        double t = h->t, dt = h->dt;
+        bool fin = h->finished;
+        while (!fin && N[i] < max_steps) {
+            ++N[i];
+            host_timestep(h->deck, t, dt, fin);
+        }
+        Scalars sc;
+        if (N[i] > 0 && ((rc = ensure_stats(h, N[i])) || (rc = read_scalars(h, &sc)))) { bad = i; break; }
+        if (N[i] > 0) { slot0[i] = sc.step; ncen[i] = sc.n_particles; }
+    }
+    FusedBatch F;
+    if (!rc && cudaStreamCreateWithFlags(&F.st, cudaStreamNonBlocking) != cudaSuccess) {
+        rc = fail(hs[0], IMC_ERR_CUDA, "cudaStreamCreateWithFlags");
+        bad = 0;
+    }
+    // launch order: the larger particle budgets first (the order is scheduling
+    // only: no deck's result depends on it)
+    std::vector<int> order((size_t)n);
+    for (int32_t i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return hs[a]->deck.n_max > hs[b]->deck.n_max; });
+    const unsigned fatal = IMC_FLAG_CAPACITY | IMC_FLAG_SEGMENT_CAP | IMC_FLAG_NAN | IMC_FLAG_FIXPOINT_RANGE |
+                           IMC_FLAG_NO_ENERGY;
+    while (!rc) {
+        std::vector<int> members;
+        for (int i : order)
+            if (done[i] < N[i]) members.push_back(i);
+        if (members.empty()) break;
+        // the largest chunk of steps whose worst-case births fit every deck's buffers
+        int64_t m = 64;
+        for (int i : members) m = std::min<int64_t>(m, N[i] - done[i]);
+        bool grew = false;
+        for (int i : members) {
+            ImcHandle *h = hs[i];
+            int64_t mi = 0;
+            long long bound = ncen[i];
+            while (mi < m) {
+                const long long nb = bound + births_bound(h, bound);
+                if (nb > h->capacity) break;
+                bound = nb;
+                ++mi;
+            }
+            if (mi == 0) {
+                if ((rc = grow(h, ncen[i] + 4 * births_bound(h, ncen[i])))) { bad = i; break; }
+                grew = true;
+            } else {
+                m = std::min(m, mi);
+            }
+        }
+        if (rc) break;
+        if (grew) {
+            F.drop();
+            continue;
+        }
+        if (!F.exec || members != F.members)
+            if ((rc = build_fused(F, hs, members, prec, &bad))) break;
+        for (int64_t s = 0; s < m && !rc; ++s) {
+            const cudaError_t e = cudaGraphLaunch(F.exec, F.st);
+            if (e != cudaSuccess) {
+                rc = fail(hs[members[0]], IMC_ERR_CUDA, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
+                bad = members[0];
+            }
+        }
+        const cudaError_t e = cudaStreamSynchronize(F.st);
+        if (!rc && e != cudaSuccess) {
+            rc = fail(hs[members[0]], IMC_ERR_CUDA, std::string("fused batch: ") + cudaGetErrorString(e));
+            bad = members[0];
+        }
+        if (rc) break;
+        bool stop = false;
+        for (int i : members) {
+            done[i] += m;
+            Scalars sc;
+            if ((rc = read_scalars(hs[i], &sc))) { bad = i; break; }
+            ncen[i] = sc.n_particles;
+            if (sc.flags & fatal) stop = true;
+        }
+        if (stop) break;
+    }
+    // host clock mirrors, totals, and each deck's own status
+    for (int32_t i = 0; i < n; ++i) {
+        unsigned fl = 0;
+        int r = absorb_steps(hs[i], slot0[i], done[i], nullptr, &fl);
+        if (steps) steps[i] = done[i];
+        if (!r) r = flags_status(hs[i], fl);
+        if (r && !rc) { rc = r; bad = i; }
+    }
+    const auto t1 = std::chrono::steady_clock::now();
+    if (wall_ms) *wall_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    if (failed) *failed = rc ? bad : -1;
+    return rc;
 }
 
 int imc_get_totals(const ImcHandle *h, int64_t *segments, int64_t *histories, int64_t *surrogate_calls) {

@@ -98,6 +98,37 @@ template <> struct Rand<double> {
     }
 };
 
+// The reference's Float64 angle 2 pi rand rounded to binary32, for the 24-bit
+// uniforms of Rand<float>::u (u = m 2^-24, m = the stream word >> 8):
+// RN32(RN64(2 pi_64 u)) = fma(m, hi, RN32(m lo)) 2^-24, where hi + lo is
+// 2 pi_64 split into binary32 (hi = RN32(2 pi_64), lo = RN32(2 pi_64 - hi)).
+// No FP64 operation; equal for every m < 2^24 (exhaustive host check in
+// tests/test_device_header.py).
+IMC_HD float two_pi_u24(uint32_t m) {
+    const float mf = (float)m;
+    return fmaf(mf, 0x1.921fb6p+2f, mf * -0x1.777a5cp-23f) * 0x1p-24f;
+}
+
+// The reference's cut-off energy 0.01 E0, a Float64 product, rounded to the
+// arithmetic type.  Binary32 without FP64 where the cut-off is a normal
+// number: with hi + lo the binary32 split of 0.01_64 (hi = RN32(0.01_64), lo
+// = RN32(0.01_64 - hi)), RN32(RN64(0.01_64 E0)) = fma(E0, hi, RN32(E0 lo))
+// for E0 >= 2^-114, and the same of E0 2^64, times 2^-64, for 0x1.9p-120 <=
+// E0 < 2^-114.  Smaller E0 (a subnormal cut-off), negative and NaN take the
+// FP64 product in a call kept out of line, so the common path holds no FP64
+// registers.  The whole function equals the FP64 form for every
+// non-negative binary32 and infinity (host check in
+// tests/test_device_header.py).
+static __host__ __device__ __noinline__ float cutoff_energy_fp64(float e0) { return (float)(0.01 * (double)e0); }
+IMC_HD float cutoff_energy(float e0) {
+    const bool tiny = e0 < 0x1p-114f;
+    const float xs = tiny ? e0 * 0x1p64f : e0;
+    const float y = fmaf(xs, 0x1.47ae14p-7f, xs * 0x1.eb851ep-33f);
+    if (!(e0 >= 0x1.9p-120f)) return cutoff_energy_fp64(e0);
+    return tiny ? y * 0x1p-64f : y;
+}
+IMC_HD double cutoff_energy(double e0) { return 0.01 * e0; }
+
 // ------------------------------------------------------- Julia semantics
 template <class T> IMC_HD T jmin(T a, T b) {
     if (a != a) return a;

@@ -179,6 +179,37 @@ void launch_energycheck_timestep(const CellArgs &ca, Scalars *sc, DevStats *stat
                                  cudaStream_t st);
 void launch_prepare_transport(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 const void *transport_kernel_ptr(const CellArgs &ca, int prec);
+// One deck of the fused batch transport (1D): what the transport reads of
+// its CellArgs, and its two particle buffers' 1D arrays.  The fused kernel
+// reads them from constant memory (kFusedMaxDecks entries), so that, like a
+// single deck's kernel parameters, they cost no registers in the history loop.
+struct Deck1DArgs {
+    int nx, nc, K, bc[2];
+    const double *dx;
+    double *sa, *fleck, *ss;
+    const double *scales;
+    long long *dep_acc, *rad_acc, *lost_acc;
+    double c, ds;
+    long long seg_cap;
+    unsigned long long seed;
+};
+struct PBufRaw1D {
+    void *t, *x, *ux, *E, *E0;
+    int32_t *cs;
+    uint8_t *alive;
+};
+struct PBufPair1D {
+    PBufRaw1D b[2];
+};
+constexpr int kFusedMaxDecks = 256;
+// the fused batch transport (1D, shared tallies): one launch over the first
+// n decks set by set_transport_multi_decks, block shape of the single-deck
+// shared-tally kernel, `smem` the largest deck's dynamic shared memory
+const void *transport_multi_ptr(int prec);
+int transport_multi_block(int prec);
+cudaError_t set_transport_multi_decks(const Deck1DArgs *ca, const PBufPair1D *bufs, Scalars *const *sc, int n,
+                                      cudaStream_t st);
+void launch_transport_multi(int n, int prec, int grid, int smem, cudaStream_t st);
 
 // threads per block of the per-cell / per-slot FP64 kernels: one warp, so that
 // a 2000-cell mesh spreads over 63 SMs (FP64 runs at 1/64 of the FP32 rate,

@@ -419,19 +419,22 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
     const T dtT = (T)dtd, dsT = (T)ca.ds;
     const int ns = nsurf_slots(ca), nc = ca.nc, nslots = ca.nslots;
     const double pd = 3.141592653589793;
-    // Each warp takes kEmitRun consecutive births at a time, lane l the births
+    // Each warp takes `run` consecutive births at a time, lane l the births
     // base + l + 32 i (every store coalesced).  A lane finds the slot of its
     // first birth by binary search over the slot offsets (slot = last q with
     // slot_off[q] <= j) and the later ones by galloping forward from there
     // (q + 1, q + 2, q + 4, ... then bisection): one or two loads where the
     // slot holds many births (the channel's surface segment), a few where
-    // it holds a handful (the CELLMIN births of every body cell).
-    constexpr int kEmitRun = 256;
+    // it holds a handful (the CELLMIN births of every body cell).  The run
+    // is the births per warp of the grid, rounded up to a multiple of 32 in
+    // [32, 256], so a small step's births still spread over every warp.
     const int lane = threadIdx.x & 31;
     const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long base = wid * kEmitRun; base < n_new; base += nw * kEmitRun)
-    for (int q = -1, r = 0; r < kEmitRun; r += 32) {
+    const long long per_warp = (n_new + nw - 1) / nw;
+    const int run = per_warp >= 256 ? 256 : per_warp <= 32 ? 32 : (int)((per_warp + 31) & ~31ll);
+    for (long long base = wid * run; base < n_new; base += nw * run)
+    for (int q = -1, r = 0; r < run; r += 32) {
         const long long j = base + r + lane;
         if (j >= n_new) break;
         if (q < 0) {
@@ -524,9 +527,11 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
                 iy = cell / ca.nx;
                 // binary32 widths precomputed (no per-birth conversion); the
                 // angle is the reference's Float64 2 pi rand rounded to T
+                // (binary32: two_pi_u24, the same value without FP64)
                 xpos = (sizeof(T) == 4 ? (T)ca.dxf[ix] : (T)ca.dx[ix]) * Rand<T>::u(rs) * dsT;
                 ypos = (sizeof(T) == 4 ? (T)ca.dyf[iy] : (T)ca.dy[iy]) * Rand<T>::u(rs) * dsT;
-                ang = (T)(2.0 * pd * (double)Rand<T>::u(rs));
+                if constexpr (sizeof(T) == 4) ang = two_pi_u24(rs.next() >> 8);
+                else ang = (T)(2.0 * pd * (double)Rand<T>::u(rs));
                 st = dtT * Rand<T>::u(rs);
             }
             T ux, uy;

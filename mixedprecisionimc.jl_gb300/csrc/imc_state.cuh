@@ -46,6 +46,9 @@ template <class St> struct PBuf {
     __host__ __device__ explicit PBuf(const PBufRaw &r)
         : t((S *)r.t), x((S *)r.x), y((S *)r.y), ux((S *)r.ux), uy((S *)r.uy), E((S *)r.E), E0((E0S *)r.E0),
           cs(r.cs), alive(r.alive) {}
+    __host__ __device__ explicit PBuf(const PBufRaw1D &r)
+        : t((S *)r.t), x((S *)r.x), y(nullptr), ux((S *)r.ux), uy(nullptr), E((S *)r.E), E0((E0S *)r.E0),
+          cs(r.cs), alive(r.alive) {}
 };
 
 template <class S> __device__ __forceinline__ float ld_f(const S *p) { return (float)*p; }

@@ -34,11 +34,15 @@ constexpr float kRefillSegments = 3.0f;
 // pass walks everything to its end.
 enum { kModePlain = 0, kModeList = 1, kModeResume = 2, kModeResumeLast = 3 };
 
-// TM: where the flushes go (kTallyGlobal, kTallyShared, or kTallySharedDep:
-// deposition tallies shared, census tallies global; the plain pass only)
-template <class St, int BLOCK, int TM, int MODE>
-__global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc, PBufPair bufs, SurrWave w,
-                                                       int round) {
+// The transport of one deck's list by one block (every thread calls; the
+// block's dynamic shared memory at smem_raw).  TM: where the flushes go
+// (kTallyGlobal, kTallyShared, or kTallySharedDep: deposition tallies shared,
+// census tallies global; the plain pass only).  The block's shared tallies
+// and counters are flushed to the deck's before it returns; the caller puts a
+// barrier between two calls.
+template <class St, int BLOCK, int TM, int MODE, class CA, class BP>
+__device__ __forceinline__ void transport1d_block(const CA &ca, Scalars *sc, const BP &bufs, const SurrWave &w,
+                                                  int round, unsigned char *smem_raw) {
     constexpr bool SMT = TM != kTallyGlobal;      // deposition flushes to shared memory
     constexpr bool RAD_SMT = TM == kTallyShared;  // census flushes to shared memory
     typedef typename St::T T;
@@ -48,7 +52,6 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     const long long n = kFromQueue ? (long long)sc->qcount[2 * round + 1] : sc->n_particles;
     if (kFromQueue && n == 0) return;
     PBuf<St> pb(bufs.b[sc->cur]);
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     Tab1<T> *tab = reinterpret_cast<Tab1<T> *>(smem_raw);
     const int N = ca.nx;
     const T ds = (T)ca.ds, c = (T)ca.c;
@@ -66,13 +69,13 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     for (int i = threadIdx.x; i < N; i += blockDim.x) tab[i] = make_tab1<T>(ca.sa[i], ca.fleck[i], ca.ss[i], ca.dx[i], ds);
     __shared__ int s_sexp[16];
     load_scale_exps(ca, s_sexp);
-    if (kPause) fill_gate<T>(ca, gate, ds, c, endsteptime);
+    if constexpr (kPause) fill_gate<T>(ca, gate, ds, c, endsteptime);
     // the barrier after the table; with the gate, also whether any cell's
     // gate is open this step (each thread tests the entries it filled; every
     // block fills the whole gate, so all blocks agree): if none is, no
     // history is tested
     bool gating = false;
-    if (kPause) gating = __syncthreads_or(gate_open(ca, gate)) && sc->surr_gate != 0;
+    if constexpr (kPause) gating = __syncthreads_or(gate_open(ca, gate)) && sc->surr_gate != 0;
     else __syncthreads();
     const int b_dep = sc->b_dep, b_rad = sc->b_rad, b_lost = sc->b_lost;
     const unsigned step = sc->step;
@@ -101,7 +104,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
         cell = cs_now & 0xFFFFFF;
         k = cs_now >> 24;
         rs.init(seed, step, (uint32_t)i, stage);
-        minenergy = (T)(0.01 * (double)E0);
+        minenergy = cutoff_energy(E0);  // (T)(0.01 * (double)E0), without FP64 in binary32
         acc_s = (T)0;
         acc_c = (T)0;
         acc_cell = cell;
@@ -299,15 +302,15 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
                 pa = e < n ? pb.alive[e] : (uint8_t)0;
                 if (pa) { pcs = pb.cs[e]; pt = pb.t[e]; px = pb.x[e]; pmu = pb.ux[e]; pE = pb.E[e]; pE0 = pb.E0[e]; }
             };
-            for (long long base = warp_counter_next(&sc->work_next) * kListChunk; base < n;
-                 base = warp_counter_next(&sc->work_next) * kListChunk) {
+            for (long long base = warp_counter_next(&sc->work_next) * kListChunk1D; base < n;
+                 base = warp_counter_next(&sc->work_next) * kListChunk1D) {
                 fetch(base + lane);
-                for (int r = 0; r < kListChunk; r += 32) {
+                for (int r = 0; r < kListChunk1D; r += 32) {
                     const long long e = base + r + lane;
                     const bool a = pa != 0;
                     const int ccs = pcs;
                     t = (T)pt; x = (T)px; mu = (T)pmu; E = (T)pE; E0 = (T)pE0;
-                    if (r + 32 < kListChunk) fetch(e + 32);
+                    if (r + 32 < kListChunk1D) fetch(e + 32);
                     if (a) {
                         i = e;
                         cs = ccs;
@@ -320,9 +323,9 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
             }
         } else {
             // the list (or a resume pass's queue) in chunks from the counter
-            for (long long base = warp_counter_next(&sc->work_next) * kListChunk; base < n;
-                 base = warp_counter_next(&sc->work_next) * kListChunk)
-                for (int r = 0; r < kListChunk; r += 32)
+            for (long long base = warp_counter_next(&sc->work_next) * kListChunk1D; base < n;
+                 base = warp_counter_next(&sc->work_next) * kListChunk1D)
+                for (int r = 0; r < kListChunk1D; r += 32)
                     if (base + r + lane < n) walk(base + r + lane);
         }
     } else {
@@ -397,6 +400,47 @@ __global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc,
     finish_counters(sc, segs, killed, flags, emax_e);
 }
 
+template <class St, int BLOCK, int TM, int MODE>
+__global__ void __launch_bounds__(BLOCK) k_transport1d(CellArgs ca, Scalars *sc, PBufPair bufs, SurrWave w,
+                                                       int round) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    transport1d_block<St, BLOCK, TM, MODE>(ca, sc, bufs, w, round, smem_raw);
+}
+
+// One transport launch over the lists of many 1D decks (the fused batch,
+// imc_run_batch_fused), whose arguments sit in constant memory.  Blocks go
+// through the decks in order; a block sets up a deck (its cell table and
+// private tallies) only while the deck's work counter still has chunks, takes
+// chunks from that counter like the single-deck kernel, and flushes the
+// deck's tallies and counters before it moves on.  Every history runs the
+// single-deck code with the deck's own streams and exact tallies, so each
+// deck's result is bit-identical to its own launch's.
+__constant__ Deck1DArgs c_multi_ca[kFusedMaxDecks];
+__constant__ PBufPair1D c_multi_bufs[kFusedMaxDecks];
+__constant__ Scalars *c_multi_sc[kFusedMaxDecks];
+
+template <class St, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_transport1d_multi(int ndecks) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_go;
+    for (int d = 0; d < ndecks; ++d) {
+        Scalars *sc = c_multi_sc[d];
+        if (threadIdx.x == 0) {
+            // chunks left: 128-entry chunks for short histories, 32-entry in
+            // the refill schedule (a stale, low counter only costs a setup)
+            const long long n = *(volatile long long *)&sc->n_particles;
+            const unsigned long long used = *(volatile unsigned long long *)&sc->work_next;
+            const long long per = *(volatile float *)&sc->seg_per_hist < kRefillSegments ? kListChunk1D : 32;
+            s_go = (long long)used * per < n;
+        }
+        __syncthreads();
+        if (s_go)
+            transport1d_block<St, BLOCK, kTallyShared, kModePlain>(c_multi_ca[d], sc, c_multi_bufs[d], SurrWave{}, 0,
+                                                                    smem_raw);
+        __syncthreads();
+    }
+}
+
 // TM, where the flushes go: kTallyGlobal, kTallyShared (deposition and
 // census tallies block-private in shared memory) or kTallySharedDep (the
 // deposition tallies only; census energy, one flush per census particle, to
@@ -460,7 +504,7 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
         xi = cell0 % NX;
         yi = cell0 / NX;
         rs.init(seed, step, (uint32_t)i, kStageTransport);
-        minenergy = (T)(0.01 * (double)E0);
+        minenergy = cutoff_energy(E0);  // (T)(0.01 * (double)E0), without FP64 in binary32
         acc_s = (T)0;
         acc_c = (T)0;
         acc_cell = cell0;
@@ -567,8 +611,11 @@ __global__ void __launch_bounds__(BLOCK) k_transport2d(CellArgs ca, Scalars *sc,
         }
         if (dist == dist_col) {
             // isotropic re-emission: angle 2*pi*rand in Float64, rounded to T
-            // (FP32: the hardware sine and cosine)
-            T ang = (T)(6.283185307179586 * (double)Rand<T>::u(rs));
+            // (binary32: two_pi_u24, the same value without FP64; the
+            // hardware sine and cosine)
+            T ang;
+            if constexpr (sizeof(T) == 4) ang = two_pi_u24(rs.next() >> 8);
+            else ang = (T)(6.283185307179586 * (double)Rand<T>::u(rs));
             if constexpr (sizeof(T) == 4) __sincosf(ang, &vy, &vx);
             else m_sincos(ang, &vy, &vx);
         }
@@ -757,6 +804,33 @@ void launch_transport(const CellArgs &ca, Scalars *sc, int prec, PBufPair buf, i
     if (prec == 0) launch_of<StF64>(ca, sh, sc, buf, grid, st);
     else if (prec == 1) launch_of<StF32>(ca, sh, sc, buf, grid, st);
     else launch_of<StF16>(ca, sh, sc, buf, grid, st);
+}
+
+const void *transport_multi_ptr(int prec) {
+    if (prec == 0) return (const void *)k_transport1d_multi<StF64, kSmtBlock64>;
+    if (prec == 1) return (const void *)k_transport1d_multi<StF32, kSmtBlock32>;
+    return (const void *)k_transport1d_multi<StF16, kSmtBlock32>;
+}
+
+int transport_multi_block(int prec) { return prec == 0 ? kSmtBlock64 : kSmtBlock32; }
+
+cudaError_t set_transport_multi_decks(const Deck1DArgs *ca, const PBufPair1D *bufs, Scalars *const *sc, int n,
+                                      cudaStream_t st) {
+    if (n < 0 || n > kFusedMaxDecks) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemcpyToSymbolAsync(c_multi_ca, ca, sizeof(Deck1DArgs) * (size_t)n, 0,
+                                            cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyToSymbolAsync(c_multi_bufs, bufs, sizeof(PBufPair1D) * (size_t)n, 0, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyToSymbolAsync(c_multi_sc, sc, sizeof(Scalars *) * (size_t)n, 0, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e;
+}
+
+void launch_transport_multi(int n, int prec, int grid, int smem, cudaStream_t st) {
+    if (prec == 0) k_transport1d_multi<StF64, kSmtBlock64><<<grid, kSmtBlock64, smem, st>>>(n);
+    else if (prec == 1) k_transport1d_multi<StF32, kSmtBlock32><<<grid, kSmtBlock32, smem, st>>>(n);
+    else k_transport1d_multi<StF16, kSmtBlock32><<<grid, kSmtBlock32, smem, st>>>(n);
 }
 
 // ------------------------------------------- analog passes of the surrogate transport

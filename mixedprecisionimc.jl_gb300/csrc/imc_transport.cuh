@@ -129,6 +129,7 @@ __host__ __device__ __forceinline__ int table_bytes(const CellArgs &ca, int tsz)
     int b = ca.geometry == 1 ? 32 * ca.nx : 16 * ca.nc + 2 * tsz * (ca.nx + ca.ny);
     return (b + 15) & ~15;
 }
+__host__ __device__ __forceinline__ int table_bytes(const Deck1DArgs &ca, int) { return (32 * ca.nx + 15) & ~15; }
 
 __device__ __forceinline__ long long *tally_smem(unsigned char *smem, int table) {
     return reinterpret_cast<long long *>(smem + table);
@@ -138,7 +139,8 @@ __device__ __forceinline__ long long *tally_smem(unsigned char *smem, int table)
 // same 3-limb layout as the global accumulators) to the global ones: limb
 // q of a slot gets its word sum plus the carries out of the limb below it.
 // with_rad false: the block holds only the deposition tallies.
-__device__ __forceinline__ void flush_block_tallies(const CellArgs &ca, const long long *sm, bool with_rad) {
+template <class CA>
+__device__ __forceinline__ void flush_block_tallies(const CA &ca, const long long *sm, bool with_rad) {
     __syncthreads();
     const int n = ca.K * ca.nc;
     for (int i = threadIdx.x; i < (with_rad ? 2 * n : n); i += blockDim.x) {
@@ -184,13 +186,16 @@ __device__ __forceinline__ void flush_one(long long *acc, int slot, T v, int b, 
 
 // Work split of the transport over the particle list (or a resume pass's
 // queue): warps take chunks in order from a counter (Scalars::work_next,
-// zeroed before each transport and by each query pass) -- kListChunk-entry
-// chunks in the short-history schedule, 32-entry chunks in the refill
-// schedule -- so the blocks (one per SM) run out of work together.  Measured
-// against a fixed grid stride over 7/8 of the list with the rest from the
-// counter: the same on the slab (+0.7 %), 29 % faster transport on the 2D
-// channel, whose history costs vary along the list.
+// zeroed before each transport and by each query pass) -- kListChunk1D- or
+// kListChunk-entry chunks in the short-history schedule of the 1D and 2D
+// kernels, 32-entry chunks in the refill schedule -- so the blocks (one per
+// SM) run out of work together.  Measured against a fixed grid stride over 7/8
+// of the list with the rest from the counter: the same on the slab (+0.7 %),
+// 29 % faster transport on the 2D channel, whose history costs vary along the
+// list.  256-entry chunks: 1.7 % faster 1D transport on the slab than 128,
+// 2-4 % slower 2D transport on the channel.
 constexpr int kListChunk = 128;
+constexpr int kListChunk1D = 256;
 // the counter's next value for the warp (warp-uniform; every lane calls)
 __device__ __forceinline__ long long warp_counter_next(unsigned long long *counter) {
     unsigned long long c = 0;
@@ -297,7 +302,7 @@ __device__ __forceinline__ void finish_counters(Scalars *sc, unsigned long long 
 
 // the exponents scale_exp(scale_k) of the deck's energy scales, in shared
 // memory (every thread calls; a barrier must follow before use)
-__device__ __forceinline__ void load_scale_exps(const CellArgs &ca, int *s_sexp) {
+template <class CA> __device__ __forceinline__ void load_scale_exps(const CA &ca, int *s_sexp) {
     for (int i = threadIdx.x; i < ca.K; i += blockDim.x) s_sexp[i] = scale_exp(ca.scales[i]);
 }
 
@@ -368,7 +373,8 @@ __device__ __forceinline__ bool gate_open(const CellArgs &ca, const float *gate)
 
 // shared-memory bytes of the 1D analog kernel: table, private tallies (SMT),
 // and the per-cell gate when histories may be set aside for queries
-__host__ __device__ __forceinline__ int analog1d_smem(const CellArgs &ca, int tsz, bool smt, bool gate) {
+template <class CA>
+__host__ __device__ __forceinline__ int analog1d_smem(const CA &ca, int tsz, bool smt, bool gate) {
     return table_bytes(ca, tsz) + (smt ? 48 * ca.K * ca.nc : 0) + (gate ? ((4 * ca.nx + 15) & ~15) : 0);
 }
 

@@ -205,7 +205,7 @@ __device__ __forceinline__ void load_queued(const SurrQueue &qq, long long e, un
     h.t = (T)qq.t[e];
     h.E = (T)qq.E[e];
     h.rs.init(seed, step, (uint32_t)h.i, stage);
-    h.minenergy = (T)(0.01 * (double)h.E0);
+    h.minenergy = cutoff_energy(h.E0);  // (T)(0.01 * (double)E0)
     h.acc_s = (T)0;
     h.acc_c = (T)0;
     h.acc_cell = h.cell;

@@ -162,6 +162,8 @@ SIGNATURES = {
     "imc_run_batch": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_int64, C.c_int32, C.POINTER(C.c_int64),
                                 C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "imc_get_surrogate_active": (C.c_int, [_H, C.POINTER(C.c_int)]),
+    "imc_run_batch_fused": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_int64, C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
 }
 
 _LIB = None

@@ -330,17 +330,24 @@ def device_info():
     return {"name": name.value.decode(), "sm_count": sm.value, "cc": (ma.value, mi.value)}
 
 
-def run_batch(engines, max_steps=1 << 40, threads=32):
-    """Batched ensemble (imc_run_batch): runs every Engine to the end of its
-    clock, the decks' kernels side by side on the GPU.  Returns (steps per
-    engine, host wall seconds).  Raises ImcError naming the first failure."""
+def run_batch(engines, max_steps=1 << 40, threads=32, fused=False):
+    """Batched ensemble: runs every Engine to the end of its clock.  With
+    fused=False (imc_run_batch) `threads` host threads drive the decks' own
+    step graphs side by side on the GPU; with fused=True
+    (imc_run_batch_fused) the decks step together, one graph per step with a
+    single transport launch over every deck (1D decks of one state precision
+    without the surrogate).  Returns (steps per engine, host wall seconds).
+    Raises ImcError naming the first failure."""
     lib = _lib.load()
     n = len(engines)
     hs = (C.c_void_p * max(n, 1))(*[e.h for e in engines])
     steps = (C.c_int64 * max(n, 1))()
     wall = C.c_double()
     bad = C.c_int32(-1)
-    rc = lib.imc_run_batch(hs, n, max_steps, threads, steps, C.byref(wall), C.byref(bad))
+    if fused:
+        rc = lib.imc_run_batch_fused(hs, n, max_steps, steps, C.byref(wall), C.byref(bad))
+    else:
+        rc = lib.imc_run_batch(hs, n, max_steps, threads, steps, C.byref(wall), C.byref(bad))
     if rc != _lib.IMC_OK:
         e = engines[bad.value] if bad.value >= 0 else None
         check(rc, e.h if e else None, lib)

@@ -10,6 +10,12 @@
 //                                   (words as the signed limbs of fix_split),
 //                                   "0" where f32_words declines, and
 //                                   fix_split's "ok l0 l1 l2" after it
+//   A                            -> the m < 2^24 where two_pi_u24(m) differs
+//                                   from (float)(2 pi * (double)(m 2^-24)),
+//                                   then "done <count>"
+//   C                            -> the binary32 x >= 0 (and +inf) where
+//                                   cutoff_energy(x) differs from
+//                                   (float)(0.01 * (double)x), "done <count>"
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -64,6 +70,31 @@ int main() {
                 printf("%d %lld %lld %lld %d %lld %lld %lld\n", f ? 1 : 0, w[2], w[1], w[0], r ? 1 : 0,
                        r ? L.l0 : 0, r ? L.l1 : 0, r ? L.l2 : 0);
             }
+        } else if (cmd == "A") {
+            const double two_pi = 2.0 * 3.141592653589793;
+            long bad = 0;
+            for (uint32_t m = 0; m < (1u << 24); ++m) {
+                const float ref = (float)(two_pi * (double)((float)m * 0x1p-24f));
+                const float got = two_pi_u24(m);
+                if (std::memcmp(&ref, &got, 4) != 0) {
+                    if (bad < 8) printf("%u ", m);
+                    ++bad;
+                }
+            }
+            printf("done %ld\n", bad);
+        } else if (cmd == "C") {
+            long bad = 0;
+            for (uint32_t b = 0; b <= 0x7F800000u; ++b) {
+                float x;
+                std::memcpy(&x, &b, 4);
+                const float ref = (float)(0.01 * (double)x);
+                const float got = cutoff_energy(x);
+                if (std::memcmp(&ref, &got, 4) != 0) {
+                    if (bad < 8) printf("%a ", x);
+                    ++bad;
+                }
+            }
+            printf("done %ld\n", bad);
         } else if (cmd == "R") {
             int prec, n, K;
             in >> prec >> n;

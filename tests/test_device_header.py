@@ -148,3 +148,18 @@ def test_f32_two_word_placement_equals_fix_split(tool):
                 assert e - 23 - b < 0, (b, v, line)
     assert took > 300
 
+
+
+def test_binary32_birth_angle_equals_float64_rounding(tool):
+    """two_pi_u24 (2D births, FP32 / FP16 state) equals the reference's
+    Float64 2 pi rand rounded to binary32 for all 2^24 uniforms."""
+    out = tool(["A"])
+    assert out == ["done 0"], out
+
+
+def test_binary32_cutoff_energy_equals_float64_rounding(tool):
+    """cutoff_energy (the 1 % cut-off of FP32 / FP16 state) equals the
+    reference's Float64 0.01 E0 rounded to binary32 for every non-negative
+    binary32 and infinity (about 30 s on one core)."""
+    out = tool(["C"])
+    assert out == ["done 0"], out
