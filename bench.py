@@ -72,9 +72,9 @@ DECKS = {
            None),
 }
 # DRAM traffic of the transport kernel per algorithmic byte, from one ncu
-# capture of the half-size slab launch (bench.py --profile): 397.5 MB read +
+# capture of the half-size slab launch (bench.py --profile): 389.7 MB read +
 # written for ~410 MB of algorithmic bytes
-TRAFFIC_PER_ALGO_BYTE = 397.5 / 410.0
+TRAFFIC_PER_ALGO_BYTE = 389.7 / 410.0
 # runs behind the RMS temperature error of the headline deck: FP32 (the timed
 # runs, plus untimed ones up to this count) and FP64 (paired seeds)
 N_ERR_FP32, N_ERR_FP64 = 12, 6
@@ -648,7 +648,7 @@ def main():
                 "frac": (achieved / hbm) if (achieved and hbm) else None,
                 "traffic": TRAFFIC_PER_ALGO_BYTE * bytes_per_launch if DECK_KEY == "c2" else None,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the half-size slab "
-                                  "launch (397.5 MB for ~410 MB algorithmic), scaled to this launch's "
+                                  "launch (389.7 MB for ~410 MB algorithmic), scaled to this launch's "
                                   "algorithmic bytes",
                 "kernel": "k_transport2d<StF32>" if DECK_KEY == "c4" else "k_transport1d<StF32>", "avg_launch_ms": avg_ms, "launches": tr_n,
                 "algorithmic_bytes_per_launch": bytes_per_launch,

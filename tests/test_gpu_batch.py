@@ -70,10 +70,10 @@ def _alone(decks, overrides=None):
     return out
 
 
-def _fused_equals_alone(decks):
+def _fused_equals_alone(decks, overrides=None):
     import mpimc
-    alone = _alone(decks)
-    engines = [mpimc.Engine(i, m) for i, m in decks]
+    alone = _alone(decks, overrides)
+    engines = [mpimc.Engine(i, m, overrides) for i, m in decks]
     steps, wall = mpimc.run_batch(engines, fused=True)
     assert wall > 0.0
     for e, s, (n, T, R, tot) in zip(engines, steps, alone):
@@ -89,6 +89,12 @@ def test_fused_batch_equals_one_by_one(gpu_lib):
     segment count equal its own run's, bit for bit (FP32 state)."""
     from c5_decks import c5_decks
     _fused_equals_alone(c5_decks(12, particle_scale=0.01))
+
+
+def test_fused_batch_fp64_equals_one_by_one(gpu_lib):
+    """FP64 state (512-thread blocks of the FP64 kernel)."""
+    from c5_decks import c5_decks
+    _fused_equals_alone(c5_decks(4, particle_scale=0.01), {"precision": 0, "scale_select_precision": 0})
 
 
 def test_fused_batch_fp16_equals_one_by_one(gpu_lib):
