@@ -522,12 +522,14 @@ PBufPair1D pair1d(const ImcHandle *h) {
 
 // Builds the step graph over `members`: every deck's update + sourcing, one
 // fused transport launch over all of them, then every deck's compaction and
-// tally + energycheck + timestep.  *bad: the deck whose capture failed.
+// tally + energycheck + timestep.  *bad: the deck whose capture failed (the
+// first member for a failure of the batch as a whole, whose message it holds).
 int build_fused(FusedBatch &F, ImcHandle *const *hs, const std::vector<int> &members, int prec, int *bad) {
     F.drop();
     F.members.clear();
     const int n = (int)members.size();
     ImcHandle *h0 = hs[members[0]];
+    *bad = members[0];
     std::vector<Deck1DArgs> cas((size_t)n);
     std::vector<PBufPair1D> bufs((size_t)n);
     std::vector<Scalars *> scs((size_t)n);
