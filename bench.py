@@ -567,6 +567,26 @@ def profile_learned_case():
     return 0
 
 
+def profile_fused_case():
+    """The first 64 decks of the 256-deck ensemble at a quarter of their
+    particle counts, stepped together 12 times with imc_run_batch_fused (one
+    transport launch per step over all 64 decks); for ncu captures of the
+    fused transport (k_transport1d_multi) and the step's launch list."""
+    import mpimc
+    from mpimc import _build
+    _build.build()
+    sys.path.insert(0, GOLDEN)
+    from c5_decks import c5_decks
+    engines = [mpimc.Engine(i, m) for i, m in c5_decks(64, particle_scale=0.25)]
+    steps, wall = mpimc.run_batch(engines, max_steps=12, fused=True)
+    tot = [e.totals() for e in engines]
+    print(json.dumps({"profile_case": "c5 first 64 decks x 0.25, fused", "steps": steps[0],
+                      "segments": int(sum(t[0] for t in tot)), "histories": int(sum(t[1] for t in tot))}))
+    for e in engines:
+        e.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -585,12 +605,16 @@ def main():
                     help="profiling case for ncu: the deck at half the particle counts, 12 timesteps, then exit")
     ap.add_argument("--profile-learned", action="store_true",
                     help="profiling case for ncu: the thick slab with the learned surrogate, 10 timesteps, then exit")
+    ap.add_argument("--profile-fused", action="store_true",
+                    help="profiling case for ncu: 64 ensemble decks stepped together (fused batch), 12 steps, then exit")
     args = ap.parse_args()
     select_deck(args.deck)
     if args.profile:
         return profile_case()
     if args.profile_learned:
         return profile_learned_case()
+    if args.profile_fused:
+        return profile_fused_case()
     rank, world, local = _env_rank()
     if world > 1:
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
