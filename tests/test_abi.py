@@ -55,3 +55,27 @@ def test_invalid_deck_rejected_before_device_use(gpu_lib):
     d.n_scales = 2
     d.abi_version = 99
     assert gpu_lib.imc_create(C.byref(d), C.byref(h)) == 1
+
+
+def test_batch_entry_points_reject_bad_lists_before_device_use(gpu_lib):
+    """Both batch entry points check the handle list before touching any
+    handle: NULL list, empty list, a NULL handle, a handle given twice, and
+    (fused) more decks than its constant-memory table holds."""
+    fake = [C.c_void_p(0x1000 + 0x100 * i) for i in range(257)]
+
+    def arr(ptrs):
+        return (C.c_void_p * len(ptrs))(*[p.value if p is not None else None for p in ptrs])
+
+    steps = (C.c_int64 * 257)()
+    wall, bad = C.c_double(), C.c_int32()
+    fused = gpu_lib.imc_run_batch_fused
+    assert fused(None, 1, 10, steps, C.byref(wall), C.byref(bad)) == 1
+    assert fused(arr(fake[:1]), 0, 10, steps, C.byref(wall), C.byref(bad)) == 1
+    assert fused(arr(fake), 257, 10, steps, C.byref(wall), C.byref(bad)) == 1
+    assert fused(arr([fake[0], None]), 2, 10, steps, C.byref(wall), C.byref(bad)) == 1
+    assert fused(arr([fake[0], fake[0]]), 2, 10, steps, C.byref(wall), C.byref(bad)) == 1
+    side = gpu_lib.imc_run_batch
+    assert side(None, 1, 10, 4, steps, C.byref(wall), C.byref(bad)) == 1
+    assert side(arr([fake[0], None]), 2, 10, 4, steps, C.byref(wall), C.byref(bad)) == 1
+    assert side(arr([fake[0], fake[0]]), 2, 10, 4, steps, C.byref(wall), C.byref(bad)) == 1
+    assert side(arr(fake[:1]), 1, 10, 0, steps, C.byref(wall), C.byref(bad)) == 1
