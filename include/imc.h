@@ -236,8 +236,9 @@ int imc_run_batch(ImcHandle *const *hs, int32_t n, int64_t max_steps, int32_t n_
  * is bit-identical to imc_run's.  The decks step together; a deck whose clock
  * ends leaves the group.  Requires every handle 1D, on one device, of one
  * state precision, without the surrogate, and with its tallies in shared
- * memory (up to 2560 cells for FP32 or FP16 state with one energy scale), at most 256 decks; otherwise
- * IMC_ERR_INVALID_ARG with *failed = the first handle that does not qualify.
+ * memory (up to 2560 cells for FP32 or FP16 state with one energy scale);
+ * otherwise IMC_ERR_INVALID_ARG with *failed = the first handle that does
+ * not qualify.  At most 256 decks per call (IMC_ERR_INVALID_ARG beyond).
  * Arguments and results as imc_run_batch; the batch stops at the first deck
  * that raises an error flag.  No counterpart in the reference (a loop over
  * its decks is the user's). */
