@@ -28,8 +28,10 @@ One bench step is one full simulation (t = 0 -> 3).  Printed on one JSON line:
   c4           the 2D channel through thick walls, FP32 state against plain
                FP64, relerr over the heated cells against
                tests/golden/c4_fp64_mean.npz, and the 2D transport roofline
-  c5           the 256-deck batched ensemble (tests/golden/c5_decks.py) run
-               side by side: learned + FP32 and plain FP32 throughput over all
+  c5           the 256-deck batched ensemble (tests/golden/c5_decks.py):
+               side by side (learned + FP32, plain FP32) and fused (plain FP32,
+               one transport launch per step over all decks, checked
+               bit-identical to the side-by-side run) throughput over all
                decks, per-deck error and FOM against plain FP64 on 16 decks
   e2e          segments/s through the public API with host buffers: deck
                upload, run and the read-back of the cell fields per step
