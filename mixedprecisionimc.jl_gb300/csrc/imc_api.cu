@@ -694,6 +694,17 @@ int imc_create(const ImcDeck *d, ImcHandle **out) {
         wf.assign(h->ny, 1.0f);
         if (d->geometry == IMC_GEOM_2D) for (int j = 0; j < h->ny; ++j) wf[j] = (float)d->dy[j];
         if ((rc = upload(h, &fp, wf.data(), h->ny))) return bail(rc); ca.dyf = fp;
+        // surface birth positions: frac * width * DISTANCESCALE in Float64 with
+        // the width and scale first rounded to the arithmetic type
+        const double fr[6] = {0.01, 0.99, 0.001, 0.999, 0.001, 0.999};
+        const double w[6] = {d->dx[0], d->dx[h->nx - 1], d->dx[0], d->dx[h->nx - 1],
+                             d->geometry == IMC_GEOM_2D ? d->dy[0] : 1.0,
+                             d->geometry == IMC_GEOM_2D ? d->dy[h->ny - 1] : 1.0};
+        const float dsf = (float)d->distancescale;
+        for (int q = 0; q < 6; ++q) {
+            ca.surf_f[q] = (float)(fr[q] * (double)(float)w[q] * (double)dsf);
+            ca.surf_d[q] = fr[q] * w[q] * d->distancescale;
+        }
     }
     if ((rc = upload(h, &ca.temp, d->temp, nc))) return bail(rc);
     if ((rc = upload(h, &ca.bee, d->bee, nc))) return bail(rc);

@@ -109,6 +109,19 @@ IMC_HD float two_pi_u24(uint32_t m) {
     return fmaf(mf, 0x1.921fb6p+2f, mf * -0x1.777a5cp-23f) * 0x1p-24f;
 }
 
+// The reference's Float64 angles -pi rand and pi (1/2 - rand) of the 2D
+// surface births, rounded to binary32, for the 24-bit uniforms u = m 2^-24:
+// each is pi_64 n 2^-24 for an integer n (1/2 - u = (2^23 - m) 2^-24 exactly
+// in binary64), and RN32(RN64(pi_64 n 2^-24)) = fma(n, hi, RN32(n lo)) 2^-24
+// with hi + lo the binary32 split of pi_64 for every |n| <= 2^24 (n itself
+// exact in binary32; exhaustive host check in tests/test_device_header.py).
+// pi (1/2 + rand) reaches n = 2^24 + 2^23, beyond that, and keeps its FP64
+// product.
+IMC_HD float pi_n24(int n) {
+    const float nf = (float)n;
+    return fmaf(nf, 0x1.921fb6p+1f, nf * -0x1.777a5cp-24f) * 0x1p-24f;
+}
+
 // The reference's cut-off energy 0.01 E0, a Float64 product, rounded to the
 // arithmetic type.  Binary32 without FP64 where the cut-off is a normal
 // number: with hi + lo the binary32 split of 0.01_64 (hi = RN32(0.01_64), lo

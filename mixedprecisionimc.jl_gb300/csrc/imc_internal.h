@@ -71,6 +71,14 @@ struct CellArgs {
     double *slot_e, *slot_s, *slot_nrg, *slot_q;
     float *slot_nrg_f;                 // slot_nrg rounded to binary32 (FP32 / FP16 births)
     const float *dxf, *dyf;            // cell widths rounded to binary32 (FP32 / FP16 births)
+    // fixed positions of the surface births, in binary32 (FP32 / FP16 state)
+    // and binary64, each the reference's Float64 product rounded to the
+    // arithmetic type: 1D 0.01 / 0.99 of the end cells
+    // (src/imc_sourcing.jl:163,178), 2D 0.001 / 0.999 of the first / last
+    // column (x, :300,315) and row (y, :271,286); order x1 left, x1 right,
+    // x2 left, x2 right, y2 bottom, y2 top
+    float surf_f[6];
+    double surf_d[6];
     int *slot_j;
     long long *slot_n, *slot_off;
     // per-block partial sums (double-double pairs) and maxima

@@ -419,6 +419,10 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
     const T dtT = (T)dtd, dsT = (T)ca.ds;
     const int ns = nsurf_slots(ca), nc = ca.nc, nslots = ca.nslots;
     const double pd = 3.141592653589793;
+    // the surface births' fixed positions, the same for every birth of a
+    // face (computed on the host, CellArgs::surf_f / surf_d)
+    auto surf = [&](int w) -> T { return sizeof(T) == 4 ? (T)ca.surf_f[w] : (T)ca.surf_d[w]; };
+    const T x1_l = surf(0), x1_r = surf(1), x2_l = surf(2), x2_r = surf(3), y2_b = surf(4), y2_t = surf(5);
     // Each warp takes `run` consecutive births at a time, lane l the births
     // base + l + 32 i (every store coalesced).  A lane finds the slot of its
     // first birth by binary search over the slot offsets (slot = last q with
@@ -469,8 +473,7 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
             if (q < 2) {
                 // surface births (src/imc_sourcing.jl:161-189)
                 const int cell = q == 0 ? 0 : ca.nx - 1;
-                const double frac = q == 0 ? 0.01 : 0.99;
-                T xpos = (T)(frac * (double)(T)ca.dx[cell] * (double)dsT);
+                T xpos = q == 0 ? x1_l : x1_r;
                 T mu = (T)0;
                 for (int r = 0; r < 64 && mu == (T)0; ++r) {
                     T rr = RT<T>::sqrt_(Rand<T>::u(rs));
@@ -501,24 +504,37 @@ __global__ void __launch_bounds__(256) k_source_emit(CellArgs ca, Scalars *sc, P
                 else if (q < 2 * nx + ny) { face = 2; idx = q - 2 * nx; }
                 else { face = 3; idx = q - 2 * nx - ny; }
                 st = dtT * Rand<T>::u(rs);
+                // the angles are the reference's Float64 products rounded to T
+                // (binary32: pi_n24 of the uniform's integer m, the same value
+                // without FP64; the widths binary32 copies)
                 if (face < 2) {
                     ix = idx;
                     iy = face == 0 ? 0 : ny - 1;
                     xpos = (sizeof(T) == 4 ? (T)ca.dxf[ix] : (T)ca.dx[ix]) * Rand<T>::u(rs) * dsT;
-                    ypos = face == 0 ? (T)(0.001 * (double)(T)ca.dy[0] * (double)dsT)
-                                     : (T)(0.999 * (double)(T)ca.dy[ny - 1] * (double)dsT);
-                    T u = Rand<T>::u(rs);
-                    ang = face == 0 ? (T)((T)pd * u) : (T)(-pd * (double)u);
+                    ypos = face == 0 ? y2_b : y2_t;
+                    if constexpr (sizeof(T) == 4) {
+                        const uint32_t m = rs.next() >> 8;
+                        ang = face == 0 ? (T)pd * ((T)m * 0x1p-24f) : -pi_n24((int)m);
+                    } else {
+                        T u = Rand<T>::u(rs);
+                        ang = face == 0 ? (T)((T)pd * u) : (T)(-pd * (double)u);
+                    }
                 } else {
                     iy = idx;
                     ix = face == 2 ? 0 : nx - 1;
-                    xpos = face == 2 ? (T)(0.001 * (double)(T)ca.dx[0] * (double)dsT)
-                                     : (T)(0.999 * (double)(T)ca.dx[nx - 1] * (double)dsT);
+                    xpos = face == 2 ? x2_l : x2_r;
                     // the reference scales y by mesh.dx[j] (src/imc_sourcing.jl:301,316)
-                    const double wq = iy < nx ? ca.dx[iy] : ca.dy[iy];
-                    ypos = (T)wq * Rand<T>::u(rs) * dsT;
-                    T u = Rand<T>::u(rs);
-                    ang = face == 2 ? (T)(pd * (0.5 - (double)u)) : (T)(pd * (0.5 + (double)u));
+                    if constexpr (sizeof(T) == 4) {
+                        ypos = (iy < nx ? ca.dxf[iy] : ca.dyf[iy]) * Rand<T>::u(rs) * dsT;
+                        const uint32_t m = rs.next() >> 8;
+                        ang = face == 2 ? pi_n24((1 << 23) - (int)m)
+                                        : (T)(pd * (0.5 + (double)((T)m * 0x1p-24f)));
+                    } else {
+                        const double wq = iy < nx ? ca.dx[iy] : ca.dy[iy];
+                        ypos = (T)wq * Rand<T>::u(rs) * dsT;
+                        T u = Rand<T>::u(rs);
+                        ang = face == 2 ? (T)(pd * (0.5 - (double)u)) : (T)(pd * (0.5 + (double)u));
+                    }
                 }
             } else {
                 // body / source births (src/imc_sourcing.jl:326-366)

@@ -13,6 +13,9 @@
 //   A                            -> the m < 2^24 where two_pi_u24(m) differs
 //                                   from (float)(2 pi * (double)(m 2^-24)),
 //                                   then "done <count>"
+//   B                            -> the m < 2^24 where a 2D surface-birth angle
+//                                   from pi_n24 differs from the Float64 form
+//                                   (faces 1 and 2), then "done <count>"
 //   C                            -> the binary32 x >= 0 (and +inf) where
 //                                   cutoff_energy(x) differs from
 //                                   (float)(0.01 * (double)x), "done <count>"
@@ -77,6 +80,19 @@ int main() {
                 const float ref = (float)(two_pi * (double)((float)m * 0x1p-24f));
                 const float got = two_pi_u24(m);
                 if (std::memcmp(&ref, &got, 4) != 0) {
+                    if (bad < 8) printf("%u ", m);
+                    ++bad;
+                }
+            }
+            printf("done %ld\n", bad);
+        } else if (cmd == "B") {
+            const double pd = 3.141592653589793;
+            long bad = 0;
+            for (uint32_t m = 0; m < (1u << 24); ++m) {
+                const float u = (float)m * 0x1p-24f;
+                const float r1 = (float)(-pd * (double)u), g1 = -pi_n24((int)m);
+                const float r2 = (float)(pd * (0.5 - (double)u)), g2 = pi_n24((1 << 23) - (int)m);
+                if (std::memcmp(&r1, &g1, 4) || std::memcmp(&r2, &g2, 4)) {
                     if (bad < 8) printf("%u ", m);
                     ++bad;
                 }

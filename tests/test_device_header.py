@@ -163,3 +163,11 @@ def test_binary32_cutoff_energy_equals_float64_rounding(tool):
     binary32 and infinity (about 30 s on one core)."""
     out = tool(["C"])
     assert out == ["done 0"], out
+
+
+def test_binary32_surface_birth_angles_equal_float64_rounding(tool):
+    """pi_n24 (2D surface births, FP32 / FP16 state) gives the reference's
+    Float64 angles -pi u and pi (1/2 - u) rounded to binary32 for all 2^24
+    uniforms u."""
+    out = tool(["B"])
+    assert out == ["done 0"], out
