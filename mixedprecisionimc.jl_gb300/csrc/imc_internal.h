@@ -183,8 +183,6 @@ void launch_finalize_tally(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 // finalize + tally + energycheck + timestep in one launch (the step sequence)
 void launch_tally_check_timestep(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap,
                                  cudaStream_t st);
-void launch_energycheck_timestep(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap,
-                                 cudaStream_t st);
 void launch_prepare_transport(const CellArgs &ca, Scalars *sc, cudaStream_t st);
 const void *transport_kernel_ptr(const CellArgs &ca, int prec);
 // One deck of the fused batch transport (1D): what the transport reads of
@@ -210,14 +208,14 @@ struct PBufPair1D {
     PBufRaw1D b[2];
 };
 constexpr int kFusedMaxDecks = 256;
-// the fused batch transport (1D, shared tallies): one launch over the first
-// n decks set by set_transport_multi_decks, block shape of the single-deck
-// shared-tally kernel, `smem` the largest deck's dynamic shared memory
+// the fused batch transport (1D, shared tallies): a kernel taking the number
+// of decks, launched (as a graph kernel node) with transport_multi_block
+// threads per block and the largest deck's dynamic shared memory over the
+// decks set by set_transport_multi_decks
 const void *transport_multi_ptr(int prec);
 int transport_multi_block(int prec);
 cudaError_t set_transport_multi_decks(const Deck1DArgs *ca, const PBufPair1D *bufs, Scalars *const *sc, int n,
                                       cudaStream_t st);
-void launch_transport_multi(int n, int prec, int grid, int smem, cudaStream_t st);
 
 // threads per block of the per-cell / per-slot FP64 kernels: one warp, so that
 // a 2000-cell mesh spreads over 63 SMs (FP64 runs at 1/64 of the FP32 rate,

@@ -1016,11 +1016,6 @@ void launch_tally_check_timestep(const CellArgs &ca, Scalars *sc, DevStats *stat
     k_tally_check<<<ca.nblk_cell, kCellThreads, 0, st>>>(ca, sc, stats, stats_cap);
 }
 
-void launch_energycheck_timestep(const CellArgs &ca, Scalars *sc, DevStats *stats, long long stats_cap,
-                                 cudaStream_t st) {
-    k_energycheck<true><<<1, 32 * (ca.K + 1), 0, st>>>(ca, sc, stats, stats_cap);
-}
-
 // Transport of a list that was set directly (no sourcing this step): take the
 // fixed-point exponents from the census maximum.
 __global__ void k_prepare_transport(CellArgs ca, Scalars *sc) {

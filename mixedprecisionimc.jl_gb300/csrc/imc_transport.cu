@@ -827,11 +827,6 @@ cudaError_t set_transport_multi_decks(const Deck1DArgs *ca, const PBufPair1D *bu
     return e;
 }
 
-void launch_transport_multi(int n, int prec, int grid, int smem, cudaStream_t st) {
-    if (prec == 0) k_transport1d_multi<StF64, kSmtBlock64><<<grid, kSmtBlock64, smem, st>>>(n);
-    else if (prec == 1) k_transport1d_multi<StF32, kSmtBlock32><<<grid, kSmtBlock32, smem, st>>>(n);
-    else k_transport1d_multi<StF16, kSmtBlock32><<<grid, kSmtBlock32, smem, st>>>(n);
-}
 
 // ------------------------------------------- analog passes of the surrogate transport
 // which: 0 the list pass, 1 a resume pass that sets aside, 2 the last resume pass
